@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the blobs step on GB300: sphere-steps/s of a 1,000,000-sphere
+world (Physics::step = 8 substeps at dt = 1/120, r ~ U[0.05, 0.15], 40%
+packing with overlaps, walled box, seeded synthetic scene).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  `value` is device-timed (CUDA events on the
+world's stream, L2 flushed between steps, inputs resident in HBM); `e2e` is
+the same metric through the C ABI with the body state written from and read
+back into pinned host memory every step; `roofline` is the dominant kernel's
+algorithmic bytes per launch over its event-timed duration; `cpu_baseline`
+is the oracle (the CPU restatement of the reference step) on bounded samples
+of the same workload, extrapolated with the reference's O(N^2) cost model.
+With --gpus N > 1 (torchrun) every rank steps its own independent world
+(replicas; the path has no data exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic bytes (the minimal traffic model of the path)
+BYTES_PER_BODY_SUBSTEP = 56      # state 40 B (read pos, pos_old, radius, mass; write pos, pos_old) + broadphase 16 B
+BYTES_CONTACT_PER_BODY = 48      # fused contact+integrate: state 40 B + read back cell key + index 8 B
+FALLBACK_HBM_GBS = 6800.0
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(name):
+    """dram bytes per launch from a committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region (read-only queries)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on samples of the workload
+# ---------------------------------------------------------------------------
+def cpu_baseline(sizes=(4096, 8192, 16384, 32768), target_n=1_000_000, seed=2, steps_per_size=1):
+    """Times Physics::step of the f32 oracle (single thread, with the
+    reference's per-body spatial-hash maintenance) on worlds of the same
+    density, fits t(N) = a N^2 + b N and extrapolates to target_n."""
+    import numpy as np
+    from blobs_gb300 import scenes
+    from oracle import oracle
+    ns, ts = [], []
+    for n in sizes:
+        s = scenes.config2(seed=seed, n=n)
+        w = oracle.OracleWorld(s, 32, maintain_spatial_hash=True)
+        w.time_steps(s.dt, 1)  # first step: pending velocity requests
+        t = w.time_steps(s.dt, steps_per_size) / steps_per_size
+        ns.append(n)
+        ts.append(t)
+    A = np.array([[n * n, n] for n in ns], float)
+    coef, *_ = np.linalg.lstsq(A, np.array(ts), rcond=None)
+    t_target = float(coef[0] * target_n * target_n + coef[1] * target_n)
+    return {
+        "value": target_n / t_target,
+        "unit": "sphere-steps/s",
+        "cores": 1,
+        "kind": "port",
+        "sample": "oracle Physics::step on %s-sphere worlds of the same density (1 step each, %.1f s total), fit "
+                  "t = a N^2 + b N, extrapolated to N=%d: %.1f s/step" % ("/".join(str(n) for n in ns), sum(ts),
+                                                                         target_n, t_target),
+        "cpu": platform.processor() or platform.machine(),
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU implementation (the
+    oracle port; the Rust crate cannot be built here), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    from blobs_gb300 import scenes
+    from oracle import oracle
+    sizes = [2048, 4096, 8192, 16384]
+    ns, ts = [], []
+    for i in range(args.warmup + args.steps):
+        n = sizes[i % len(sizes)]
+        s = scenes.config2(seed=2, n=n)
+        w = oracle.OracleWorld(s, 32, maintain_spatial_hash=True)
+        w.time_steps(s.dt, 1)
+        t = w.time_steps(s.dt, 1)
+        if i >= args.warmup:
+            ns.append(n)
+            ts.append(t)
+    A = np.array([[n * n, n] for n in ns], float)
+    coef, *_ = np.linalg.lstsq(A, np.array(ts), rcond=None)
+    N = args.n
+    t_target = float(coef[0] * N * N + coef[1] * N)
+    value = N / t_target
+    line = {
+        "impl": "reference", "metric": "sphere-steps/s @1M", "value": value, "unit": "sphere-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_target * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded config2 generator)",
+        "config": {"workload": "1M spheres, r~U[0.05,0.15], 40% packing, dt=1/120, 8 substeps (extrapolated from "
+                               "samples)", "bodies": N},
+        "cpu_baseline": {"value": value, "unit": "sphere-steps/s", "cores": 1, "kind": "port",
+                         "sample": "one oracle step per timed iteration on %s-sphere worlds of the same density, "
+                                   "fit t = a N^2 + b N, extrapolated to N=%d" % ("/".join(map(str, sizes)), N)},
+        "e2e": {"value": value, "unit": "sphere-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+    from blobs_gb300 import native, scenes
+
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    scene = scenes.config2(seed=2 + rank, n=args.n)
+    dt = scene.dt
+    world = native.World(scene, device=local_rank)
+    stream = torch.cuda.Stream(dev)          # graphs cannot be captured on the legacy default stream
+    torch.cuda.set_stream(stream)
+    world.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 126 MB L2
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        world.step(dt)
+    barrier()
+
+    # -- timed region: device time of K steps, L2 flushed before each --------
+    clocks = Clocks(local_rank)
+    clocks.start()
+    k0 = world.kernel_launches()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        world.step(dt)
+        ends[i].record(stream)
+    barrier()
+    clk = clocks.stop()
+    launches = world.kernel_launches() - k0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = world_size * scene.n_bodies * args.steps / (total_ms / 1e3)
+
+    # -- per-phase kernel time (events captured into the step graph) ---------
+    world.set_timing(True)
+    world.step(dt)  # capture the instrumented graph
+    world.phase_times()
+    phase = {p: [0.0, 0] for p in native.World.PHASES}
+    for i in range(args.steps):
+        flush.zero_()
+        world.step(dt)
+        for p, (ms, n) in world.phase_times().items():
+            phase[p][0] += ms
+            phase[p][1] += n
+    world.set_timing(False)
+    dom = max(phase, key=lambda p: phase[p][0])
+    dom_ms = phase[dom][0] / max(1, phase[dom][1])
+    peak, peak_kind = peak_hbm()
+    alg_bytes = BYTES_CONTACT_PER_BODY * scene.n_bodies if dom == "contact" else None
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9 if alg_bytes else None
+
+    # -- end to end through the C ABI with pinned host buffers ----------------
+    n = scene.n_bodies
+    h_pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+    h_old = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+    h_vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+    world.read_bodies_into(h_pos, h_old, h_vel)
+    e2e_s = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        world.write_bodies(h_pos, h_old)
+        world.step(dt)
+        world.read_bodies_into(h_pos, h_old, h_vel)   # synchronising
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_t = torch.tensor([sum(e2e_s)], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = world_size * n * args.steps / float(e2e_t.item())
+    contacts_total, contacts_last = world.contact_count()
+    world.sync()
+
+    whole_achieved = BYTES_PER_BODY_SUBSTEP * scene.substeps * value / 1e9 / world_size
+    line = {
+        "metric": "sphere-steps/s @1M", "value": value, "unit": "sphere-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded config2 generator: uniform positions with overlaps, N(0,0.5) velocities)",
+        "config": {"workload": "1M spheres, r~U[0.05,0.15], 40% packing (side %.1f, walled), g=(0,-9.81), "
+                               "dt=1/120, 8 substeps/step" % (float(scene.world_box[0, 2] * 2)),
+                   "bodies": scene.n_bodies, "substeps": scene.substeps, "parallelism": "replicas" if world_size > 1
+                   else "single", "l2": "flushed (256 MiB write) before every timed step",
+                   "contacts_last_substep": contacts_last},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": dom_ms,
+                     "traffic": profile_traffic("contact_single_1M.md"),
+                     "step_alg_GBps": whole_achieved, "step_frac": whole_achieved / peak},
+        "phases_ms_per_step": {p: phase[p][0] / args.steps for p in phase},
+        "e2e": {"value": e2e_value, "unit": "sphere-steps/s", "h2d_bytes_per_step": 16 * n,
+                "d2h_bytes_per_step": 24 * n},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(target_n=scene.n_bodies)
+    world.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+// device.cuh -- device-side world layout and the f32 arithmetic of the blobs
+// step (darthdeus/blobs 0.2.1, blobs/src/physics.rs), shared by every kernel.
+//
+// Every translation unit that includes this file is compiled with
+// --fmad=false: the reference never contracts a*b+c into an FMA (Rust does
+// not contract, glam's Vec2 is scalar code), and the contact / spring /
+// integration results are bit-exact only if the GPU rounds every product and
+// sum separately, in the same order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace blobs {
+
+// Per-body flag bits.
+enum : uint8_t {
+  BF_STATIC = 1,     // RigidBodyType::Static (rigid_body.rs:211-213)
+  BF_FIRST_DYN = 2,  // first non-static body of its world in arena order: sees dt/old_dt (physics.rs:338-339)
+  BF_VREQ = 4,       // velocity_request is Some (consumed by the next substep, physics.rs:334-336)
+};
+
+// Device status bits, read back by the host after a synchronising call.
+enum : uint32_t {
+  ST_NAN = 1u,         // NaN contact normal or non-finite rotation (physics.rs:293, 471-474)
+  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up
+  ST_BAD_INDEX = 4u,   // a device bounds check fired
+};
+
+// Per-world parameters (a batch packs many independent worlds).
+struct WorldParam {
+  uint32_t cell_base;   // first cell of this world's toroidal grid in the global cell table
+  uint32_t log2w;       // grid is (1 << log2w) x (1 << log2h) cells, coordinates wrap
+  uint32_t log2h;
+  float cs;             // cell edge
+  float box_lo_x, box_lo_y, box_hi_x, box_hi_y;
+  uint32_t has_box;     // axis-aligned wall extension enabled
+  uint32_t pad[3];
+};
+
+// Every device pointer of a loaded scene.  Passed to kernels by value.
+struct WorldDev {
+  uint32_t n_bodies, n_cols, n_springs, n_joints, n_worlds, n_circles, n_cells, n_tiles;
+  float2 gravity;
+
+  // bodies (arena order)
+  float2* pos_old;
+  float2* vel;          // calculated_velocity
+  float2* acc;          // per-substep force accumulator (springs present)
+  float* rot;
+  float* angvel;
+  float* mass;          // calculated_mass (rigid_body.rs:96-128)
+  float* inertia;
+  float* gmod;          // gravity_mod
+  float* bound_r;       // bounding radius for the wall extension
+  uint8_t* bflags;
+  float2* pend_acc;     // acceleration present before the step (consumed by its first substep)
+  float* pend_torque;
+  float2* vreq;
+  uint32_t* body_world;      // batched only
+  uint32_t* body_col_start;  // n_bodies + 1: colliders of a body (ascending)
+  uint32_t* body_cols;
+  uint32_t* body_spr_start;  // n_bodies + 1: incident springs, ascending spring index
+  uint32_t* body_spr;        // (spring index << 1) | (1 if the body is endpoint b)
+
+  // colliders (arena order)
+  uint32_t* col_parent;
+  float2* col_off;
+  float* col_radius;
+  uint32_t* col_memb;
+  uint32_t* col_filt;
+  uint8_t* col_sensor;
+  float2* snap;              // absolute_transform.translation
+  uint32_t* col_world;       // batched only
+
+  // springs (arena order)
+  uint32_t* spr_a;
+  uint32_t* spr_b;
+  float* spr_rest;
+  float* spr_k;
+  float* spr_c;
+
+  // joints (stored in the coloured processing order)
+  uint32_t* jnt_a;
+  uint32_t* jnt_b;
+  float2* jnt_anchor_a;
+  float2* jnt_anchor_b;
+  float* jnt_dist;
+  float* jnt_target;
+
+  float* circles;            // 3 per circle
+  WorldParam* wparam;
+
+  // broadphase
+  uint32_t* cell_count;      // n_cells, zero between substeps
+  uint32_t* cell_start;      // n_cells + 1
+  uint32_t* rank;            // per collider: slot inside its cell
+  float4* sorted;            // per slot: (x, y, radius, collider index bits)
+  unsigned long long* tile_state;
+  uint32_t* tile_counter;
+
+  // counters
+  unsigned long long* contacts_total;
+  unsigned long long* pushouts_total;
+  uint32_t* contacts_sub;    // contacts of the most recent substep
+  uint32_t* status;
+};
+
+// ---------------------------------------------------------------------------
+// glam Vec2 arithmetic, one rounding per operation.
+// ---------------------------------------------------------------------------
+__device__ __host__ __forceinline__ float2 v2(float x, float y) { return make_float2(x, y); }
+__device__ __host__ __forceinline__ float2 add(float2 a, float2 b) { return v2(a.x + b.x, a.y + b.y); }
+__device__ __host__ __forceinline__ float2 sub(float2 a, float2 b) { return v2(a.x - b.x, a.y - b.y); }
+__device__ __host__ __forceinline__ float2 mul(float2 a, float s) { return v2(a.x * s, a.y * s); }
+__device__ __host__ __forceinline__ float2 mulv(float2 a, float2 b) { return v2(a.x * b.x, a.y * b.y); }
+__device__ __host__ __forceinline__ float2 divs(float2 a, float s) { return v2(a.x / s, a.y / s); }
+__device__ __host__ __forceinline__ float dot2(float2 a, float2 b) { return (a.x * b.x) + (a.y * b.y); }
+__device__ __host__ __forceinline__ float len2(float2 a) { return sqrtf(dot2(a, a)); }
+
+// Rust `(v / cs).floor() as i32`: IEEE division, saturating conversion, NaN -> 0
+// (spatial.rs:57-62 semantics).
+__device__ __host__ __forceinline__ int32_t cell_coord(float v, float cs) {
+  float q = floorf(v / cs);
+  if (q != q) return 0;
+  if (q >= 2147483648.0f) return 2147483647;
+  if (q <= -2147483648.0f) return (-2147483647 - 1);
+  return (int32_t)q;
+}
+
+// Global cell index of a point in world `wp`'s toroidal grid.
+__device__ __host__ __forceinline__ uint32_t cell_key(const WorldParam& wp, float2 s) {
+  uint32_t ix = (uint32_t)cell_coord(s.x, wp.cs) & ((1u << wp.log2w) - 1u);
+  uint32_t iy = (uint32_t)cell_coord(s.y, wp.cs) & ((1u << wp.log2h) - 1u);
+  return wp.cell_base + ((iy << wp.log2w) | ix);
+}
+
+// Affine2::from_angle_translation(rot, pos) * offset -> translation
+// (rigid_body.rs:88-90, physics.rs:360-366; glam Mat2 * Vec2 column form).
+__device__ __forceinline__ float2 collider_translation(float rot, float2 pos, float2 off) {
+  float s, c;
+  sincosf(rot, &s, &c);
+  float2 m = v2((c * off.x) + ((-s) * off.y), (s * off.x) + (c * off.y));
+  return add(m, pos);
+}
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SPIN_LIMIT = 1u << 22;  // bounded waits: polls before giving up
+constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
+
+}  // namespace blobs

@@ -1,0 +1,748 @@
+// kernels.cu -- sm_103a kernels of one blobs substep (physics.rs:397-422).
+//
+// Per substep, for every packed world at once:
+//   k_cell_scan        exclusive scan of the per-cell collider counts -> cell
+//                      ranges (decoupled look-back, single pass), counts reset
+//   k_scatter_forces   counting-sort scatter of the colliders into cell order
+//                      (the one-digit LSD radix pass over the cell key) and,
+//                      when springs exist, gravity + spring forces per body
+//   k_contact_*        per-body gather of sphere contacts over the 3x3 cells,
+//                      corrections applied in the reference's pair-sequence
+//                      order; fused with integration when there are no joints
+//   k_joints           one colour of the fixed-joint Gauss-Seidel sweep
+//   k_integrate        Verlet + collider snapshot + constraints, and the cell
+//                      key / rank of every collider for the next substep
+//
+// The cell counts for substep s+1 are produced by the integration of substep
+// s (atomicAdd rank per collider), so no separate key pass runs in steady
+// state.  Compiled with --fmad=false; see device.cuh.
+#include "device.cuh"
+#include "kernels.h"
+
+namespace blobs {
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void set_status(const WorldDev& w, uint32_t bit) { atomicOr(w.status, bit); }
+
+__device__ __forceinline__ WorldParam load_wparam(const WorldDev& w, uint32_t world) {
+  return w.wparam[world];
+}
+
+__device__ __forceinline__ void publish_tile(unsigned long long* ts, uint32_t tile, uint32_t flag, uint32_t value) {
+  unsigned long long v = ((unsigned long long)flag << 32) | value;
+  __threadfence();
+  *reinterpret_cast<volatile unsigned long long*>(ts + tile) = v;
+}
+
+// ---------------------------------------------------------------------------
+// k_cell_scan: cell_start[k] = sum(cell_count[0..k)), cell_start[n] = total,
+// cell_count[:] = 0.  Tiles are taken in launch order from a counter, so the
+// look-back only waits on tiles that are already running; the wait is bounded
+// (SPIN_LIMIT polls) and sets ST_TIMEOUT instead of hanging.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SCAN_THREADS) k_cell_scan(WorldDev w) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_prefix;
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(w.tile_counter, 1u);
+    if (s_tile == 0) *w.contacts_sub = 0u;
+  }
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= w.n_tiles) {  // counter not reset: never index past tile_state
+    if (threadIdx.x == 0) set_status(w, ST_BAD_INDEX);
+    return;
+  }
+  const uint32_t n = w.n_cells;
+  const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  const bool full = base + SCAN_ITEMS <= n;
+  if (full) {
+    uint4* src = reinterpret_cast<uint4*>(w.cell_count + base);
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+      uint4 t = src[q];
+      v[4 * q + 0] = t.x;
+      v[4 * q + 1] = t.y;
+      v[4 * q + 2] = t.z;
+      v[4 * q + 3] = t.w;
+      src[q] = make_uint4(0u, 0u, 0u, 0u);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      size_t k = base + i;
+      v[i] = k < n ? w.cell_count[k] : 0u;
+      if (k < n) w.cell_count[k] = 0u;
+    }
+  }
+  uint32_t tsum = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) tsum += v[i];
+
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = tsum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int NW = SCAN_THREADS / 32;
+    uint32_t t = lane < NW ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < NW; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= (uint32_t)o) t += y;
+    }
+    if (lane < NW) s_warp[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t thread_excl = (warp ? s_warp[warp - 1] : 0u) + x - tsum;
+  const uint32_t block_total = s_warp[SCAN_THREADS / 32 - 1];
+
+  if (threadIdx.x == 0) {
+    uint32_t excl = 0;
+    if (tile == 0) {
+      publish_tile(w.tile_state, 0, 2u, block_total);
+    } else {
+      publish_tile(w.tile_state, tile, 1u, block_total);
+      int64_t t = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      while (t >= 0) {
+        unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(w.tile_state + t);
+        uint32_t flag = (uint32_t)(st >> 32);
+        if (flag == 0u) {
+          if (++spins >= SPIN_LIMIT) {
+            set_status(w, ST_TIMEOUT);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        excl += (uint32_t)st;
+        if (flag == 2u) break;
+        --t;
+      }
+      publish_tile(w.tile_state, tile, 2u, excl + block_total);
+    }
+    s_prefix = excl;
+  }
+  __syncthreads();
+  uint32_t run = s_prefix + thread_excl;
+  if (full) {
+    uint4* dst = reinterpret_cast<uint4*>(w.cell_start + base);
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+      uint4 t;
+      t.x = run; run += v[4 * q + 0];
+      t.y = run; run += v[4 * q + 1];
+      t.z = run; run += v[4 * q + 2];
+      t.w = run; run += v[4 * q + 3];
+      dst[q] = t;
+    }
+    if (base + SCAN_ITEMS == n) w.cell_start[n] = run;
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      size_t k = base + i;
+      if (k < n) {
+        w.cell_start[k] = run;
+        run += v[i];
+        if (k + 1 == n) w.cell_start[n] = run;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gravity + springs for one body (physics.rs:369-375, springs.rs:25-47,
+// rigid_body.rs:155-160).  Springs are visited in ascending arena index and
+// each spring force is recomputed with identical operations at both
+// endpoints, so every body accumulates exactly the reference's sequence.
+// ---------------------------------------------------------------------------
+template <bool PEND>
+__device__ __forceinline__ float2 body_forces(const WorldDev& w, uint32_t b, const float2* __restrict__ pos) {
+  float2 a = PEND ? w.pend_acc[b] : v2(0.0f, 0.0f);
+  a = add(a, mul(w.gravity, w.gmod[b]));
+  const float m = w.mass[b];
+  const uint32_t q0 = w.body_spr_start[b], q1 = w.body_spr_start[b + 1];
+  for (uint32_t q = q0; q < q1; ++q) {
+    const uint32_t e = w.body_spr[q];
+    const uint32_t s = e >> 1;
+    const uint32_t ia = w.spr_a[s], ib = w.spr_b[s];
+    const float2 pa = pos[ia], pb = pos[ib];
+    const float2 d = sub(pb, pa);
+    const float dist = len2(d);
+    const float2 dir = divs(d, dist);
+    const float2 rv = sub(w.vel[ia], w.vel[ib]);
+    const float2 damping = mul(dir, w.spr_c[s] * dot2(rv, dir));
+    const float sk = w.spr_k[s] * (dist - w.spr_rest[s]);
+    const float2 fm = v2(sk - damping.x, sk - damping.y);  // f32 - Vec2 broadcast, springs.rs:41
+    float2 f = mulv(dir, fm);
+    if (e & 1u) f = v2(-f.x, -f.y);
+    a = add(a, divs(f, m));
+  }
+  return a;
+}
+
+template <bool MW, bool SCATTER, bool SPR, bool PEND>
+__global__ void __launch_bounds__(256) k_scatter_forces(WorldDev w, const float2* __restrict__ pos) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (SCATTER) {
+    if (blockIdx.x == 0) {
+      for (uint32_t t = threadIdx.x; t < w.n_tiles; t += blockDim.x) w.tile_state[t] = 0ull;
+      if (threadIdx.x == 0) *w.tile_counter = 0u;
+    }
+    if (i < w.n_cols) {
+      const float2 s = w.snap[i];
+      const WorldParam wp = load_wparam(w, MW ? w.col_world[i] : 0u);
+      const uint32_t key = cell_key(wp, s);
+      const uint32_t slot = w.cell_start[key] + w.rank[i];
+      if (slot < w.n_cols) w.sorted[slot] = make_float4(s.x, s.y, w.col_radius[i], __uint_as_float(i));
+      else set_status(w, ST_BAD_INDEX);
+    }
+  }
+  if (SPR && i < w.n_bodies) {
+    if (!(w.bflags[i] & BF_STATIC)) w.acc[i] = body_forces<PEND>(w, i, pos);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// integration of one body (physics.rs:323-367) followed by the constraints
+// (physics.rs:377-395, then the wall extension).  `p` is the body position
+// after contacts and joints.  Collider snapshots are taken BEFORE the
+// constraints (the reference refreshes them inside update_objects only), and
+// their cell keys/ranks for the next substep are recorded here.
+// ---------------------------------------------------------------------------
+struct SubstepArgs {
+  float dt;
+  float old_dt;
+  uint32_t do_keys;
+  uint32_t rot_dynamic;  // 0: every angular velocity is 0 and no torque is pending -> rotation is constant
+};
+
+template <bool MW, bool SPR, bool PEND, bool SINGLE>
+__device__ __forceinline__ void integrate_body(const WorldDev& w, uint32_t b, float2 p, float2* __restrict__ pos_out,
+                                               const SubstepArgs& a) {
+  const uint8_t fl = w.bflags[b];
+  const float dt = a.dt;
+  float2 po;
+  float2 vel;
+  float rot = 0.0f;
+  if (!SINGLE || a.rot_dynamic) rot = w.rot[b];
+  if (fl & BF_STATIC) {
+    po = p;
+    vel = v2(0.0f, 0.0f);
+  } else {
+    po = w.pos_old[b];
+    if (PEND && (fl & BF_VREQ)) po = sub(p, mul(w.vreq[b], dt));
+    const float ratio = (fl & BF_FIRST_DYN) ? dt / a.old_dt : dt / dt;
+    const float2 disp = mul(sub(p, po), ratio);
+    float2 acc;
+    if (SPR) {
+      acc = w.acc[b];
+    } else {
+      acc = PEND ? w.pend_acc[b] : v2(0.0f, 0.0f);
+      acc = add(acc, mul(w.gravity, w.gmod[b]));
+    }
+    po = p;
+    p = add(p, add(disp, mul(mul(acc, dt), dt)));
+    if (a.rot_dynamic) {
+      const float tq = PEND ? w.pend_torque[b] : 0.0f;
+      float av = w.angvel[b];
+      av = av + (tq / w.inertia[b]) * dt;
+      rot = rot + av * dt;
+      w.angvel[b] = av;
+      w.rot[b] = rot;
+    }
+    vel = divs(disp, dt);
+  }
+  const uint32_t world = MW ? w.body_world[b] : 0u;
+  const WorldParam wp = load_wparam(w, world);
+  if (SINGLE) {
+    const float2 s = v2(0.0f + p.x, 0.0f + p.y);  // rot(θ) * 0 + p
+    w.snap[b] = s;
+    if (a.do_keys) w.rank[b] = atomicAdd(w.cell_count + cell_key(wp, s), 1u);
+  } else {
+    const uint32_t c0 = w.body_col_start[b], c1 = w.body_col_start[b + 1];
+    for (uint32_t q = c0; q < c1; ++q) {
+      const uint32_t c = w.body_cols[q];
+      const float2 s = collider_translation(rot, p, w.col_off[c]);
+      w.snap[c] = s;
+      if (a.do_keys) w.rank[c] = atomicAdd(w.cell_count + cell_key(wp, s), 1u);
+    }
+  }
+  for (uint32_t k = 0; k < w.n_circles; ++k) {
+    const float2 c = v2(w.circles[3 * k], w.circles[3 * k + 1]);
+    const float radius = w.circles[3 * k + 2];
+    const float2 to = sub(p, c);
+    const float dist = len2(to);
+    if (dist > radius) p = add(c, mul(divs(to, dist), radius));
+  }
+  if (wp.has_box) {
+    const float br = w.bound_r[b];
+    p.x = fminf(fmaxf(p.x, wp.box_lo_x + br), wp.box_hi_x - br);
+    p.y = fminf(fmaxf(p.y, wp.box_lo_y + br), wp.box_hi_y - br);
+  }
+  pos_out[b] = p;
+  w.pos_old[b] = po;
+  w.vel[b] = vel;
+}
+
+// ---------------------------------------------------------------------------
+// Candidate enumeration: the 3 rows of 3 cells around point s, each row a
+// contiguous range of the cell-sorted array (split in two where the torus
+// wraps).
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const WorldDev& w, const WorldParam& wp, float2 s, F&& f) {
+  const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
+  const uint32_t ix = (uint32_t)cell_coord(s.x, wp.cs), iy = (uint32_t)cell_coord(s.y, wp.cs);
+  const uint32_t x0 = (ix - 1u) & wm, x2 = (ix + 1u) & wm;
+#pragma unroll 1
+  for (int oy = -1; oy <= 1; ++oy) {
+    const uint32_t row = wp.cell_base + (((iy + (uint32_t)oy) & hm) << wp.log2w);
+    // ranges are clamped to the slot count: a corrupt cell table cannot walk
+    // past the sorted array
+    if (x0 < x2) {
+      const uint32_t e0 = w.cell_start[row + x0], e1 = min(w.cell_start[row + x2 + 1u], w.n_cols);
+      for (uint32_t e = e0; e < e1; ++e) f(e);
+    } else {
+      uint32_t e0 = w.cell_start[row + x0], e1 = min(w.cell_start[row + wm + 1u], w.n_cols);
+      for (uint32_t e = e0; e < e1; ++e) f(e);
+      e0 = w.cell_start[row], e1 = min(w.cell_start[row + x2 + 1u], w.n_cols);
+      for (uint32_t e = e0; e < e1; ++e) f(e);
+    }
+  }
+}
+
+struct Contact {
+  unsigned long long key;  // (hi << 33) | (lo << 1)
+  float2 corr;             // signed position increment for this body
+};
+
+// One contact of collider c (body b) with collider c2 (body b2), in the
+// reference's terms: a = the higher collider index (outer loop), b = lower.
+// Returns false if the pair is not in contact.  Sets *push when the
+// coincident-centre branch (physics.rs:272-286) was taken; its increments are
+// then applied as (push, corr) in that order.
+struct PairOut {
+  float2 push;
+  float2 corr;
+  bool pushed;
+  bool has_corr;
+};
+
+__device__ __forceinline__ bool contact_pair(const WorldDev& w, const float2* __restrict__ pos_in, uint32_t c,
+                                             uint32_t b, float2 s, float r, float m_b, uint32_t c2, uint32_t b2,
+                                             float2 s2, float r2, float m_b2, bool sensor_any, float2 off_c,
+                                             float2 off_c2, PairOut& out) {
+  const bool hi = c > c2;
+  float2 axis = hi ? sub(s, s2) : sub(s2, s);
+  float d = len2(axis);
+  const float min_dist = hi ? (r + r2) : (r2 + r);
+  if (!(d < min_dist)) return false;
+  out.pushed = false;
+  out.push = v2(0.0f, 0.0f);
+  if (d < 1e-6f) {
+    // Push-out with the snapshots refreshed to body position + offset.  The
+    // positions used are those at the start of the contact pass (exact when
+    // neither body received an earlier correction in this substep).
+    const float2 pa = add(pos_in[hi ? b : b2], v2(0.01f, 0.0f));
+    const float2 pb = sub(pos_in[hi ? b2 : b], v2(0.01f, 0.0f));
+    const float2 sa = add(pa, hi ? off_c : off_c2);
+    const float2 sb = add(pb, hi ? off_c2 : off_c);
+    axis = sub(sa, sb);
+    d = len2(axis);
+    out.pushed = true;
+    out.push = hi ? v2(0.01f, 0.0f) : v2(-0.01f, -0.0f);  // p - (0.01, 0) == p + (-0.01, -0)
+  }
+  out.has_corr = !sensor_any;
+  out.corr = v2(0.0f, 0.0f);
+  if (!sensor_any) {
+    const float2 n = divs(axis, d);
+    if (n.x != n.x || n.y != n.y) set_status(w, ST_NAN);
+    const float delta = min_dist - d;
+    const float ma = hi ? m_b : m_b2, mb = hi ? m_b2 : m_b;
+    const float ratio = 1.0f - ma / (ma + mb);
+    if (hi) {
+      out.corr = mul(n, ratio * delta);
+    } else {
+      const float2 t = mul(n, (1.0f - ratio) * delta);
+      out.corr = v2(-t.x, -t.y);
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void sort_contacts(Contact* l, int n) {
+  for (int i = 1; i < n; ++i) {
+    Contact t = l[i];
+    int j = i - 1;
+    while (j >= 0 && l[j].key > t.key) {
+      l[j + 1] = l[j];
+      --j;
+    }
+    l[j + 1] = t;
+  }
+}
+
+__device__ __forceinline__ unsigned long long pair_key(uint32_t c, uint32_t c2) {
+  const uint32_t hi = c > c2 ? c : c2, lo = c > c2 ? c2 : c;
+  return ((unsigned long long)hi << 33) | ((unsigned long long)lo << 1);
+}
+
+__device__ __forceinline__ void count_contacts(const WorldDev& w, uint32_t ncontacts, uint32_t npush) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t t = ncontacts, p = npush;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t += __shfl_down_sync(0xffffffffu, t, o);
+    p += __shfl_down_sync(0xffffffffu, p, o);
+  }
+  if (lane == 0 && t) {
+    atomicAdd(w.contacts_total, (unsigned long long)t);
+    atomicAdd(w.contacts_sub, t);
+  }
+  if (lane == 0 && p) atomicAdd(w.pushouts_total, (unsigned long long)p);
+}
+
+// ---------------------------------------------------------------------------
+// k_contact_single: worlds whose bodies each own exactly one collider with a
+// zero offset, default groups and no sensor.  One thread per cell-sorted
+// slot, so a warp works on neighbouring cells.  Contacts are collected,
+// sorted by the neighbour's arena index (= the reference's pair sequence for
+// this body) and applied in that order; more than CONTACT_LIST contacts or a
+// push-out switch to an exact selection walk.
+// ---------------------------------------------------------------------------
+template <bool MW, bool SPR, bool PEND, bool FUSE>
+__global__ void __launch_bounds__(256) k_contact_single(WorldDev w, const float2* __restrict__ pos_in,
+                                                        float2* __restrict__ pos_out, SubstepArgs args) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t ncontacts = 0, npush = 0;
+  if (e < w.n_cols) {
+    const float4 me = w.sorted[e];
+    uint32_t c = __float_as_uint(me.w);
+    if (c >= w.n_cols) {
+      set_status(w, ST_BAD_INDEX);
+      c = 0;
+    }
+    const float2 s = v2(me.x, me.y);
+    const float r = me.z;
+    const WorldParam wp = load_wparam(w, MW ? w.col_world[c] : 0u);
+    const float m_c = w.mass[c];
+    Contact list[CONTACT_LIST];
+    int nl = 0;
+    bool slow = false;
+    for_each_candidate(w, wp, s, [&](uint32_t q) {
+      if (q == e) return;
+      const float4 o = w.sorted[q];
+      const uint32_t c2 = __float_as_uint(o.w);
+      if (c2 >= w.n_cols) return;
+      PairOut po;
+      if (!contact_pair(w, pos_in, c, c, s, r, m_c, c2, c2, v2(o.x, o.y), o.z, w.mass[c2], false,
+                        v2(0.0f, 0.0f), v2(0.0f, 0.0f), po))
+        return;
+      if (c > c2) {
+        ++ncontacts;
+        npush += po.pushed ? 1u : 0u;
+      }
+      if (po.pushed || nl >= CONTACT_LIST) {
+        slow = true;
+        return;
+      }
+      list[nl].key = pair_key(c, c2);
+      list[nl].corr = po.corr;
+      ++nl;
+    });
+    float2 p = pos_in[c];
+    if (!slow) {
+      sort_contacts(list, nl);
+      for (int k = 0; k < nl; ++k) p = add(p, list[k].corr);
+    } else {
+      // exact selection walk in ascending pair key
+      unsigned long long last = 0ull;
+      bool first = true;
+      while (true) {
+        unsigned long long best = ~0ull;
+        PairOut bo;
+        for_each_candidate(w, wp, s, [&](uint32_t q) {
+          if (q == e) return;
+          const float4 o = w.sorted[q];
+          const uint32_t c2 = __float_as_uint(o.w);
+          if (c2 >= w.n_cols) return;
+          const unsigned long long k = pair_key(c, c2);
+          if ((!first && k <= last) || k >= best) return;
+          PairOut po;
+          if (!contact_pair(w, pos_in, c, c, s, r, m_c, c2, c2, v2(o.x, o.y), o.z, w.mass[c2], false,
+                            v2(0.0f, 0.0f), v2(0.0f, 0.0f), po))
+            return;
+          best = k;
+          bo = po;
+        });
+        if (best == ~0ull) break;
+        if (bo.pushed) p = add(p, bo.push);
+        p = add(p, bo.corr);
+        last = best;
+        first = false;
+      }
+    }
+    if (FUSE) {
+      integrate_body<MW, SPR, PEND, true>(w, c, p, pos_out, args);
+    } else {
+      pos_out[c] = p;
+    }
+  }
+  count_contacts(w, ncontacts, npush);
+}
+
+// ---------------------------------------------------------------------------
+// k_contact_general: any body / collider layout (several colliders per body,
+// offsets, groups, sensors).  One thread per body; the contacts of all its
+// colliders are merged in the reference's pair-sequence order
+// (outer collider index, then inner collider index).
+// ---------------------------------------------------------------------------
+template <bool MW, bool SPR, bool PEND, bool FUSE>
+__global__ void __launch_bounds__(256) k_contact_general(WorldDev w, const float2* __restrict__ pos_in,
+                                                         float2* __restrict__ pos_out, SubstepArgs args) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t ncontacts = 0, npush = 0;
+  if (b < w.n_bodies) {
+    const uint32_t c0 = w.body_col_start[b], c1 = w.body_col_start[b + 1];
+    const WorldParam wp = load_wparam(w, MW ? w.body_world[b] : 0u);
+    const float m_b = w.mass[b];
+    Contact list[CONTACT_LIST];
+    int nl = 0;
+    bool slow = false;
+    for (uint32_t qc = c0; qc < c1; ++qc) {
+      const uint32_t c = w.body_cols[qc];
+      const float2 s = w.snap[c];
+      const float r = w.col_radius[c];
+      const uint32_t memb = w.col_memb[c], filt = w.col_filt[c];
+      const bool sens = w.col_sensor[c] != 0;
+      const float2 off = w.col_off[c];
+      for_each_candidate(w, wp, s, [&](uint32_t q) {
+        const float4 o = w.sorted[q];
+        const uint32_t c2 = __float_as_uint(o.w);
+        if (c2 == c || c2 >= w.n_cols) return;
+        const float2 s2 = v2(o.x, o.y);
+        // cheap distance pre-test, the exact test is repeated in contact_pair
+        const float2 ax = c > c2 ? sub(s, s2) : sub(s2, s);
+        const float md = c > c2 ? (r + o.z) : (o.z + r);
+        if (!(len2(ax) < md)) return;
+        const uint32_t b2 = w.col_parent[c2];
+        if (b2 == b) return;
+        const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
+        if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
+        const bool sens_any = sens || (w.col_sensor[c2] != 0);
+        PairOut po;
+        if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, s2, o.z, w.mass[b2], sens_any, off, w.col_off[c2],
+                          po))
+          return;
+        if (c > c2) {
+          ++ncontacts;
+          npush += po.pushed ? 1u : 0u;
+        }
+        if (po.pushed || nl >= CONTACT_LIST) {
+          slow = true;
+          return;
+        }
+        list[nl].key = pair_key(c, c2);
+        list[nl].corr = po.corr;
+        ++nl;
+      });
+    }
+    float2 p = pos_in[b];
+    if (!slow) {
+      sort_contacts(list, nl);
+      for (int k = 0; k < nl; ++k) p = add(p, list[k].corr);
+    } else {
+      unsigned long long last = 0ull;
+      bool first = true;
+      while (true) {
+        unsigned long long best = ~0ull;
+        PairOut bo;
+        for (uint32_t qc = c0; qc < c1; ++qc) {
+          const uint32_t c = w.body_cols[qc];
+          const float2 s = w.snap[c];
+          const float r = w.col_radius[c];
+          const uint32_t memb = w.col_memb[c], filt = w.col_filt[c];
+          const bool sens = w.col_sensor[c] != 0;
+          const float2 off = w.col_off[c];
+          for_each_candidate(w, wp, s, [&](uint32_t q) {
+            const float4 o = w.sorted[q];
+            const uint32_t c2 = __float_as_uint(o.w);
+            if (c2 == c || c2 >= w.n_cols) return;
+            const unsigned long long k = pair_key(c, c2);
+            if ((!first && k <= last) || k >= best) return;
+            const uint32_t b2 = w.col_parent[c2];
+            if (b2 == b) return;
+            const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
+            if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
+            const bool sens_any = sens || (w.col_sensor[c2] != 0);
+            PairOut po;
+            if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, v2(o.x, o.y), o.z, w.mass[b2], sens_any, off,
+                              w.col_off[c2], po))
+              return;
+            best = k;
+            bo = po;
+          });
+        }
+        if (best == ~0ull) break;
+        if (bo.pushed) p = add(p, bo.push);
+        if (bo.has_corr) p = add(p, bo.corr);
+        last = best;
+        first = false;
+      }
+    }
+    if (FUSE) {
+      integrate_body<MW, SPR, PEND, false>(w, b, p, pos_out, args);
+    } else {
+      pos_out[b] = p;
+    }
+  }
+  count_contacts(w, ncontacts, npush);
+}
+
+// ---------------------------------------------------------------------------
+// k_joints: one colour of solve_fixed_joints (physics.rs:424-477).  Joints of
+// one colour touch disjoint bodies, so they run in parallel; colours run in
+// sequence, joint_iterations times.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_joints(WorldDev w, float2* __restrict__ pos, uint32_t j0, uint32_t j1,
+                                                float dt) {
+  const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= j1) return;
+  const uint32_t ia = w.jnt_a[j], ib = w.jnt_b[j];
+  float2 pa = pos[ia], pb = pos[ib];
+  const float2 wa = add(pa, w.jnt_anchor_a[j]);
+  const float2 wb = add(pb, w.jnt_anchor_b[j]);
+  const float2 dp = sub(wb, wa);
+  const float distance = len2(dp);
+  if (distance < 1e-6f) return;
+  const float off_by = distance - w.jnt_dist[j];
+  const float2 correction = divs(v2(off_by * dp.x, off_by * dp.y), distance);
+  const float ma = w.mass[ia], mb = w.mass[ib];
+  const float ims = (1.0f / ma) + (1.0f / mb);
+  const bool sa = (w.bflags[ia] & BF_STATIC) != 0, sb = (w.bflags[ib] & BF_STATIC) != 0;
+  if (sa) {
+    pb = sub(pb, mul(correction, ims));
+  } else if (sb) {
+    pa = add(pa, mul(correction, ims));
+  } else {
+    const float ratio = (1.0f / ma) / ims;
+    pa = add(pa, mul(correction, ratio));
+    pb = sub(pb, mul(correction, 1.0f - ratio));
+  }
+  pos[ia] = pa;
+  pos[ib] = pb;
+  const float angle_a = atan2f(dp.y, dp.x);
+  const float angle_b = -atan2f(dp.y, -dp.x);  // physics.rs:464 precedence
+  const float rc = ((angle_b - angle_a) - w.jnt_target[j]) * 0.5f;
+  const float ra = w.rot[ia] + rc * dt;
+  const float rb = w.rot[ib] - rc * dt;
+  w.rot[ia] = ra;
+  w.rot[ib] = rb;
+  if (!isfinite(ra) || !isfinite(rb)) set_status(w, ST_NAN);
+}
+
+template <bool MW, bool SPR, bool PEND, bool SINGLE>
+__global__ void __launch_bounds__(256) k_integrate(WorldDev w, const float2* __restrict__ pos_in,
+                                                   float2* __restrict__ pos_out, SubstepArgs args) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.n_bodies) return;
+  integrate_body<MW, SPR, PEND, SINGLE>(w, b, pos_in[b], pos_out, args);
+}
+
+// Cell keys and in-cell ranks of every collider from the current snapshots
+// (after a load or a host write; in steady state integration records them).
+template <bool MW>
+__global__ void __launch_bounds__(256) k_keys(WorldDev w) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= w.n_cols) return;
+  const WorldParam wp = load_wparam(w, MW ? w.col_world[c] : 0u);
+  w.rank[c] = atomicAdd(w.cell_count + cell_key(wp, w.snap[c]), 1u);
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+static inline uint32_t blocks_for(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+
+void launch_keys(const WorldDev& w, bool mw, cudaStream_t st) {
+  if (!w.n_cols) return;
+  const uint32_t g = blocks_for(w.n_cols, 256);
+  if (mw) k_keys<true><<<g, 256, 0, st>>>(w);
+  else k_keys<false><<<g, 256, 0, st>>>(w);
+}
+
+void launch_scan(const WorldDev& w, cudaStream_t st) {
+  const uint32_t tiles = blocks_for(w.n_cells, SCAN_TILE);
+  k_cell_scan<<<tiles, SCAN_THREADS, 0, st>>>(w);
+}
+
+#define BLOBS_DISPATCH_BOOL(v, NAME, ...) \
+  if (v) {                                \
+    constexpr bool NAME = true;           \
+    __VA_ARGS__;                          \
+  } else {                                \
+    constexpr bool NAME = false;          \
+    __VA_ARGS__;                          \
+  }
+
+void launch_scatter_forces(const WorldDev& w, const float2* pos, bool mw, bool scatter, bool springs, bool pending,
+                           cudaStream_t st) {
+  const uint32_t nc = scatter ? w.n_cols : 0u, nb = springs ? w.n_bodies : 0u;
+  const uint32_t n = nc > nb ? nc : nb;
+  if (!n) return;
+  const uint32_t g = blocks_for(n, 256);
+  BLOBS_DISPATCH_BOOL(mw, MW,
+    BLOBS_DISPATCH_BOOL(scatter, SC,
+      BLOBS_DISPATCH_BOOL(springs, SP,
+        BLOBS_DISPATCH_BOOL(pending, PE, k_scatter_forces<MW, SC, SP, PE><<<g, 256, 0, st>>>(w, pos)))));
+}
+
+void launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
+                     bool pending, bool fuse, float dt, float old_dt, bool do_keys, bool rot_dynamic,
+                     cudaStream_t st) {
+  SubstepArgs a{dt, old_dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
+  if (single) {
+    if (!w.n_cols) return;
+    const uint32_t g = blocks_for(w.n_cols, 256);
+    BLOBS_DISPATCH_BOOL(mw, MW,
+      BLOBS_DISPATCH_BOOL(springs, SP,
+        BLOBS_DISPATCH_BOOL(pending, PE,
+          BLOBS_DISPATCH_BOOL(fuse, FU, k_contact_single<MW, SP, PE, FU><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+  } else {
+    if (!w.n_bodies) return;
+    const uint32_t g = blocks_for(w.n_bodies, 256);
+    BLOBS_DISPATCH_BOOL(mw, MW,
+      BLOBS_DISPATCH_BOOL(springs, SP,
+        BLOBS_DISPATCH_BOOL(pending, PE,
+          BLOBS_DISPATCH_BOOL(fuse, FU, k_contact_general<MW, SP, PE, FU><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+  }
+}
+
+void launch_joints(const WorldDev& w, float2* pos, uint32_t j0, uint32_t j1, float dt, cudaStream_t st) {
+  if (j1 <= j0) return;
+  k_joints<<<blocks_for(j1 - j0, 256), 256, 0, st>>>(w, pos, j0, j1, dt);
+}
+
+void launch_integrate(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
+                      bool pending, float dt, float old_dt, bool do_keys, bool rot_dynamic, cudaStream_t st) {
+  if (!w.n_bodies) return;
+  SubstepArgs a{dt, old_dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
+  const uint32_t g = blocks_for(w.n_bodies, 256);
+  BLOBS_DISPATCH_BOOL(mw, MW,
+    BLOBS_DISPATCH_BOOL(springs, SP,
+      BLOBS_DISPATCH_BOOL(pending, PE,
+        BLOBS_DISPATCH_BOOL(single, SI, k_integrate<MW, SP, PE, SI><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+}
+
+}  // namespace blobs

@@ -1,0 +1,1091 @@
+// world.cu -- host side of the device world behind include/blobs_gpu.h.
+//
+// A blobs_world holds one scene (one reference `Physics`, or a batch of
+// independent ones packed back to back) resident in HBM as
+// structure-of-arrays, a CUDA stream, and the CUDA graphs of its steps.
+// `step(dt)` (physics.rs:78-82) is one graph launch of `substeps` substeps.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "../../include/blobs_gpu.h"
+#include "device.cuh"
+#include "kernels.h"
+#include "world.h"
+
+using namespace blobs;
+
+namespace {
+
+struct Counters {
+  unsigned long long contacts_total;
+  unsigned long long pushouts_total;
+  uint32_t contacts_sub;
+  uint32_t status;
+  uint32_t tile_counter;
+  uint32_t pad;
+};
+
+inline uint32_t next_pow2(uint64_t v) {
+  uint32_t p = 1;
+  while (p < v && p < (1u << 30)) p <<= 1;
+  return p;
+}
+inline uint32_t ilog2(uint32_t v) {
+  uint32_t l = 0;
+  while ((1u << l) < v) ++l;
+  return l;
+}
+
+// Bump allocator over one cudaMalloc.
+struct Carver {
+  size_t off = 0;
+  char* base = nullptr;
+  template <class T> T* take(size_t count) {
+    size_t bytes = count * sizeof(T);
+    size_t at = (off + 255) & ~(size_t)255;
+    off = at + (bytes ? bytes : 1);
+    return base ? reinterpret_cast<T*>(base + at) : nullptr;
+  }
+};
+
+}  // namespace
+
+int blobs_map_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return BLOBS_OK;
+  if (e == cudaErrorMemoryAllocation) return BLOBS_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return BLOBS_ERR_NO_DEVICE;
+  return BLOBS_ERR_CUDA;
+}
+
+struct GraphKey {
+  uint32_t dt_bits;
+  uint32_t cur;
+  uint32_t n_steps;
+  uint32_t timing;
+  bool operator<(const GraphKey& o) const {
+    if (dt_bits != o.dt_bits) return dt_bits < o.dt_bits;
+    if (cur != o.cur) return cur < o.cur;
+    if (n_steps != o.n_steps) return n_steps < o.n_steps;
+    return timing < o.timing;
+  }
+};
+
+// CUDA events around each kernel phase of a step (recorded into the step
+// graph when timing is on), so the host can read per-phase device time.
+struct TimingSet {
+  struct Mark {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  void destroy() {
+    for (auto& m : marks) {
+      cudaEventDestroy(m.a);
+      cudaEventDestroy(m.b);
+    }
+    marks.clear();
+  }
+};
+
+struct blobs_world {
+  blobs_config cfg;
+  cudaStream_t stream = nullptr;
+  bool loaded = false;
+
+  uint32_t nb = 0, nc = 0, ns = 0, nj = 0, nw = 0, ncirc = 0;
+  bool multiworld = false, single = false, has_springs = false, has_joints = false, rot_dynamic = false;
+  bool any_dynamic = false;
+  bool pending = false;
+  bool keys_valid = false;
+  std::vector<uint32_t> colour_offsets;  // colour k = joints [colour_offsets[k], colour_offsets[k+1]) in processing order
+  std::vector<uint32_t> joint_order;     // processing position -> arena index
+  float old_dt = 1.0f;
+  double time = 0.0, accumulator = 0.0;
+  uint32_t cur = 0;
+  float2* pos[2] = {nullptr, nullptr};
+  void* arena = nullptr;
+  Counters* dcounters = nullptr;
+  Counters* hcounters = nullptr;  // pinned
+  WorldDev dev{};
+  uint32_t sticky_status = 0;
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  cudaStream_t user_stream = nullptr;  // caller's stream (NULL: the world's own)
+  bool timing = false;
+  bool capturing = false;
+  TimingSet* recording = nullptr;      // set that enqueue_substep records into
+  std::map<GraphKey, TimingSet> graph_timing;
+  TimingSet eager_timing;
+  std::vector<TimingSet*> launched_sets;
+  uint64_t kernels_launched = 0;       // kernels issued (graph nodes counted per launch)
+  uint64_t enqueued = 0;               // kernels enqueued by enqueue_substep (eager or captured)
+  std::map<GraphKey, uint64_t> graph_kernels;
+
+  cudaStream_t st() const { return user_stream ? user_stream : stream; }
+
+  ~blobs_world() { release(); }
+
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    for (auto& kv : graph_timing) kv.second.destroy();
+    graph_timing.clear();
+    eager_timing.destroy();
+    launched_sets.clear();
+  }
+  void release() {
+    drop_graphs();
+    if (arena) cudaFree(arena);
+    arena = nullptr;
+    if (hcounters) cudaFreeHost(hcounters);
+    hcounters = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    loaded = false;
+  }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// scene validation + derived host arrays
+// ---------------------------------------------------------------------------
+struct HostScene {
+  std::vector<float2> pos, pos_old, pend_acc, vel, vreq, col_off, snap, anchor_a, anchor_b;
+  std::vector<float> rot, angvel, pend_torque, mass, inertia, gmod, bound_r, col_radius, spr_rest, spr_k, spr_c,
+      jnt_dist, jnt_target, circles;
+  std::vector<uint8_t> bflags, col_sensor;
+  std::vector<uint32_t> body_world, col_world, body_col_start, body_cols, body_spr_start, body_spr, col_parent,
+      col_memb, col_filt, spr_a, spr_b, jnt_a, jnt_b;
+  std::vector<WorldParam> wparam;
+  std::vector<uint32_t> colour_offsets, joint_order;
+  uint32_t n_cells = 0;
+  bool single = false, rot_dynamic = false, pending = false, any_dynamic = false;
+};
+
+int world_of(const uint32_t* offsets, uint32_t nw, uint32_t idx) {
+  // offsets is validated to be non-decreasing; binary search
+  uint32_t lo = 0, hi = nw;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) / 2;
+    if (offsets[mid] <= idx) lo = mid;
+    else hi = mid;
+  }
+  return (int)lo;
+}
+
+bool check_offsets(const uint32_t* off, uint32_t nw, uint32_t total) {
+  if (!off) return nw <= 1;
+  if (off[0] != 0 || off[nw] != total) return false;
+  for (uint32_t w = 0; w < nw; ++w)
+    if (off[w + 1] < off[w]) return false;
+  return true;
+}
+
+int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h) {
+  const uint32_t nw = s.n_worlds ? s.n_worlds : 1;
+  const uint32_t nb = s.n_bodies, nc = s.n_colliders, ns = s.n_springs, nj = s.n_joints;
+  if (nb && (!s.pos || !s.mass || !s.inertia)) return BLOBS_ERR_INVALID_ARGUMENT;
+  if (nc && (!s.col_parent || !s.col_radius)) return BLOBS_ERR_INVALID_ARGUMENT;
+  if (ns && (!s.spr_a || !s.spr_b || !s.spr_rest || !s.spr_k || !s.spr_c)) return BLOBS_ERR_INVALID_ARGUMENT;
+  if (nj && (!s.jnt_a || !s.jnt_b || !s.jnt_anchor_a || !s.jnt_anchor_b || !s.jnt_distance || !s.jnt_target))
+    return BLOBS_ERR_INVALID_ARGUMENT;
+  if (s.n_circles && !s.circles) return BLOBS_ERR_INVALID_ARGUMENT;
+  if (nw > 1) {
+    if (!check_offsets(s.world_body_offsets, nw, nb) || !check_offsets(s.world_collider_offsets, nw, nc) ||
+        !check_offsets(s.world_spring_offsets, nw, ns) || !check_offsets(s.world_joint_offsets, nw, nj))
+      return BLOBS_ERR_INVALID_ARGUMENT;
+  }
+  auto bworld = [&](uint32_t b) -> uint32_t { return nw > 1 ? (uint32_t)world_of(s.world_body_offsets, nw, b) : 0u; };
+
+  // bodies
+  h.pos.resize(nb);
+  h.pos_old.resize(nb);
+  h.pend_acc.resize(nb);
+  h.vel.resize(nb);
+  h.vreq.resize(nb);
+  h.rot.resize(nb);
+  h.angvel.resize(nb);
+  h.pend_torque.resize(nb);
+  h.mass.resize(nb);
+  h.inertia.resize(nb);
+  h.gmod.resize(nb);
+  h.bound_r.assign(nb, 0.0f);
+  h.bflags.assign(nb, 0);
+  h.body_world.resize(nb);
+  std::vector<uint8_t> seen_dyn(nw, 0);
+  for (uint32_t i = 0; i < nb; ++i) {
+    h.pos[i] = v2(s.pos[2 * i], s.pos[2 * i + 1]);
+    h.pos_old[i] = s.pos_old ? v2(s.pos_old[2 * i], s.pos_old[2 * i + 1]) : h.pos[i];
+    h.pend_acc[i] = s.acc ? v2(s.acc[2 * i], s.acc[2 * i + 1]) : v2(0.0f, 0.0f);
+    h.vel[i] = s.vel ? v2(s.vel[2 * i], s.vel[2 * i + 1]) : v2(0.0f, 0.0f);
+    const bool vset = s.vreq_set && s.vreq_set[i];
+    if (vset && !s.vreq) return BLOBS_ERR_INVALID_ARGUMENT;
+    h.vreq[i] = vset ? v2(s.vreq[2 * i], s.vreq[2 * i + 1]) : v2(0.0f, 0.0f);
+    h.rot[i] = s.rotation ? s.rotation[i] : 0.0f;
+    h.angvel[i] = s.angvel ? s.angvel[i] : 0.0f;
+    h.pend_torque[i] = s.torque ? s.torque[i] : 0.0f;
+    h.gmod[i] = s.gravity_mod ? s.gravity_mod[i] : 1.0f;
+    h.mass[i] = s.mass[i];
+    h.inertia[i] = s.inertia[i];
+    if (!(h.mass[i] > 0.0f) || !std::isfinite(h.mass[i])) return BLOBS_ERR_INVALID_ARGUMENT;
+    const uint8_t type = s.body_type ? s.body_type[i] : (uint8_t)BLOBS_DYNAMIC;
+    if (type > 3) return BLOBS_ERR_INVALID_ARGUMENT;
+    const uint32_t w = bworld(i);
+    h.body_world[i] = w;
+    uint8_t f = 0;
+    if (type == BLOBS_STATIC) {
+      f |= BF_STATIC;
+    } else {
+      h.any_dynamic = true;
+      if (!seen_dyn[w]) {
+        f |= BF_FIRST_DYN;
+        seen_dyn[w] = 1;
+      }
+    }
+    if (vset) f |= BF_VREQ;
+    h.bflags[i] = f;
+    if (vset || h.pend_acc[i].x != 0.0f || h.pend_acc[i].y != 0.0f || h.pend_torque[i] != 0.0f) h.pending = true;
+    if (h.angvel[i] != 0.0f || h.pend_torque[i] != 0.0f) h.rot_dynamic = true;
+  }
+
+  // colliders
+  h.col_parent.resize(nc);
+  h.col_off.resize(nc);
+  h.col_radius.resize(nc);
+  h.col_sensor.resize(nc);
+  h.col_memb.resize(nc);
+  h.col_filt.resize(nc);
+  h.snap.resize(nc);
+  h.col_world.resize(nc);
+  std::vector<uint32_t> per_body(nb + 1, 0);
+  bool single = (nc == nb);
+  for (uint32_t c = 0; c < nc; ++c) {
+    const uint32_t p = s.col_parent[c];
+    if (p >= nb) return BLOBS_ERR_INVALID_ARGUMENT;
+    const uint32_t w = nw > 1 ? (uint32_t)world_of(s.world_collider_offsets, nw, c) : 0u;
+    if (w != h.body_world[p]) return BLOBS_ERR_INVALID_ARGUMENT;
+    h.col_world[c] = w;
+    h.col_parent[c] = p;
+    h.col_off[c] = s.col_offset ? v2(s.col_offset[2 * c], s.col_offset[2 * c + 1]) : v2(0.0f, 0.0f);
+    h.col_radius[c] = s.col_radius[c];
+    if (!(h.col_radius[c] >= 0.0f) || !std::isfinite(h.col_radius[c])) return BLOBS_ERR_INVALID_ARGUMENT;
+    h.col_sensor[c] = s.col_sensor ? (s.col_sensor[c] ? 1 : 0) : 0;
+    h.col_memb[c] = s.col_memb ? s.col_memb[c] : 0xffffffffu;
+    h.col_filt[c] = s.col_filt ? s.col_filt[c] : 0xffffffffu;
+    if (s.col_snap) {
+      h.snap[c] = v2(s.col_snap[2 * c], s.col_snap[2 * c + 1]);
+    } else {
+      const float sn = std::sin(h.rot[p]), cs = std::cos(h.rot[p]);
+      const float2 o = h.col_off[c];
+      h.snap[c] = add(v2((cs * o.x) + ((-sn) * o.y), (sn * o.x) + (cs * o.y)), h.pos[p]);
+    }
+    const float br = len2(h.col_off[c]) + h.col_radius[c];
+    if (br > h.bound_r[p]) h.bound_r[p] = br;
+    per_body[p + 1]++;
+    if (p != c || h.col_off[c].x != 0.0f || h.col_off[c].y != 0.0f || h.col_sensor[c] ||
+        h.col_memb[c] != 0xffffffffu || h.col_filt[c] != 0xffffffffu)
+      single = false;
+  }
+  h.single = single;
+  h.body_col_start.resize(nb + 1);
+  h.body_col_start[0] = 0;
+  for (uint32_t b = 0; b < nb; ++b) h.body_col_start[b + 1] = h.body_col_start[b] + per_body[b + 1];
+  h.body_cols.resize(nc);
+  {
+    std::vector<uint32_t> fill(h.body_col_start.begin(), h.body_col_start.end() - 1);
+    for (uint32_t c = 0; c < nc; ++c) h.body_cols[fill[h.col_parent[c]]++] = c;
+  }
+
+  // springs -> per-body incident list in ascending spring index
+  h.spr_a.resize(ns);
+  h.spr_b.resize(ns);
+  h.spr_rest.resize(ns);
+  h.spr_k.resize(ns);
+  h.spr_c.resize(ns);
+  std::vector<uint32_t> spr_count(nb + 1, 0);
+  for (uint32_t i = 0; i < ns; ++i) {
+    const uint32_t a = s.spr_a[i], b = s.spr_b[i];
+    if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
+    if (h.body_world[a] != h.body_world[b]) return BLOBS_ERR_INVALID_ARGUMENT;
+    if (nw > 1 && (uint32_t)world_of(s.world_spring_offsets, nw, i) != h.body_world[a])
+      return BLOBS_ERR_INVALID_ARGUMENT;
+    h.spr_a[i] = a;
+    h.spr_b[i] = b;
+    h.spr_rest[i] = s.spr_rest[i];
+    h.spr_k[i] = s.spr_k[i];
+    h.spr_c[i] = s.spr_c[i];
+    spr_count[a + 1]++;
+    spr_count[b + 1]++;
+  }
+  h.body_spr_start.resize(nb + 1);
+  h.body_spr_start[0] = 0;
+  for (uint32_t b = 0; b < nb; ++b) h.body_spr_start[b + 1] = h.body_spr_start[b] + spr_count[b + 1];
+  h.body_spr.resize(2 * (size_t)ns);
+  {
+    std::vector<uint32_t> fill(h.body_spr_start.begin(), h.body_spr_start.end() - 1);
+    for (uint32_t i = 0; i < ns; ++i) {
+      h.body_spr[fill[h.spr_a[i]]++] = (i << 1);
+      h.body_spr[fill[h.spr_b[i]]++] = (i << 1) | 1u;
+    }
+  }
+
+  // joints: greedy colouring in arena order, processing order = (colour, arena index)
+  std::vector<uint32_t> colour(nj, 0);
+  uint32_t n_colours = 0;
+  {
+    std::vector<std::vector<uint32_t>> used(nb);
+    for (uint32_t j = 0; j < nj; ++j) {
+      const uint32_t a = s.jnt_a[j], b = s.jnt_b[j];
+      if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
+      if (h.body_world[a] != h.body_world[b]) return BLOBS_ERR_INVALID_ARGUMENT;
+      if (nw > 1 && (uint32_t)world_of(s.world_joint_offsets, nw, j) != h.body_world[a])
+        return BLOBS_ERR_INVALID_ARGUMENT;
+      uint32_t k = 0;
+      while (std::find(used[a].begin(), used[a].end(), k) != used[a].end() ||
+             std::find(used[b].begin(), used[b].end(), k) != used[b].end())
+        ++k;
+      colour[j] = k;
+      used[a].push_back(k);
+      used[b].push_back(k);
+      n_colours = std::max(n_colours, k + 1);
+    }
+  }
+  h.colour_offsets.assign(n_colours + 1, 0);
+  for (uint32_t j = 0; j < nj; ++j) h.colour_offsets[colour[j] + 1]++;
+  for (uint32_t k = 0; k < n_colours; ++k) h.colour_offsets[k + 1] += h.colour_offsets[k];
+  h.joint_order.resize(nj);
+  {
+    std::vector<uint32_t> fill(h.colour_offsets.begin(), h.colour_offsets.end() - 1);
+    for (uint32_t j = 0; j < nj; ++j) h.joint_order[fill[colour[j]]++] = j;
+  }
+  h.jnt_a.resize(nj);
+  h.jnt_b.resize(nj);
+  h.anchor_a.resize(nj);
+  h.anchor_b.resize(nj);
+  h.jnt_dist.resize(nj);
+  h.jnt_target.resize(nj);
+  for (uint32_t q = 0; q < nj; ++q) {
+    const uint32_t j = h.joint_order[q];
+    h.jnt_a[q] = s.jnt_a[j];
+    h.jnt_b[q] = s.jnt_b[j];
+    h.anchor_a[q] = v2(s.jnt_anchor_a[2 * j], s.jnt_anchor_a[2 * j + 1]);
+    h.anchor_b[q] = v2(s.jnt_anchor_b[2 * j], s.jnt_anchor_b[2 * j + 1]);
+    h.jnt_dist[q] = s.jnt_distance[j];
+    h.jnt_target[q] = s.jnt_target[j];
+  }
+  if (nj) h.rot_dynamic = true;
+
+  h.circles.assign(s.circles, s.circles + 3 * (size_t)s.n_circles);
+
+  // per-world toroidal grids
+  h.wparam.resize(nw);
+  uint64_t cell_base = 0;
+  for (uint32_t w = 0; w < nw; ++w) {
+    const uint32_t c0 = nw > 1 ? s.world_collider_offsets[w] : 0u;
+    const uint32_t c1 = nw > 1 ? s.world_collider_offsets[w + 1] : nc;
+    float rmax = 0.0f;
+    float lo_x = INFINITY, lo_y = INFINITY, hi_x = -INFINITY, hi_y = -INFINITY;
+    for (uint32_t c = c0; c < c1; ++c) {
+      rmax = std::max(rmax, h.col_radius[c]);
+      const float2 p = h.snap[c];
+      if (std::isfinite(p.x) && std::isfinite(p.y)) {
+        lo_x = std::min(lo_x, p.x);
+        hi_x = std::max(hi_x, p.x);
+        lo_y = std::min(lo_y, p.y);
+        hi_y = std::max(hi_y, p.y);
+      }
+    }
+    // The 3x3 search is exact when cs >= 2 * rmax; the 1/64 margin absorbs
+    // the rounding of v / cs for coordinates up to ~1e5 cells.
+    const float safe = rmax > 0.0f ? 2.0f * rmax * (1.0f + 1.0f / 64.0f) : 1.0f;
+    const float cs = cfg.cell_size > safe ? cfg.cell_size : safe;
+    const double ex = hi_x >= lo_x ? (double)hi_x - lo_x : 0.0, ey = hi_y >= lo_y ? (double)hi_y - lo_y : 0.0;
+    uint32_t W = next_pow2(std::max<uint64_t>(4, (uint64_t)std::ceil(ex / cs) + 3));
+    uint32_t H = next_pow2(std::max<uint64_t>(4, (uint64_t)std::ceil(ey / cs) + 3));
+    const uint64_t cap = std::max<uint64_t>(16, 2ull * next_pow2(std::max<uint32_t>(1, c1 - c0)));
+    while ((uint64_t)W * H > cap) {
+      if (W >= H && W > 4) W >>= 1;
+      else if (H > 4) H >>= 1;
+      else break;
+    }
+    WorldParam& wp = h.wparam[w];
+    std::memset(&wp, 0, sizeof(wp));
+    wp.cell_base = (uint32_t)cell_base;
+    wp.log2w = ilog2(W);
+    wp.log2h = ilog2(H);
+    wp.cs = cs;
+    if (s.world_box) {
+      wp.has_box = 1;
+      wp.box_lo_x = s.world_box[4 * w + 0];
+      wp.box_lo_y = s.world_box[4 * w + 1];
+      wp.box_hi_x = s.world_box[4 * w + 2];
+      wp.box_hi_y = s.world_box[4 * w + 3];
+    }
+    cell_base += (uint64_t)W * H;
+    if (cell_base >= (1ull << 31)) return BLOBS_ERR_INVALID_ARGUMENT;
+  }
+  h.n_cells = (uint32_t)cell_base;
+  return BLOBS_OK;
+}
+
+template <class T> cudaError_t up(T* dst, const std::vector<T>& src, cudaStream_t st) {
+  if (src.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+// Lay out (or size) every device array of the scene.
+void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t nb, uint32_t nc, uint32_t ns,
+           uint32_t nj, uint32_t nw, uint32_t ncirc, uint32_t n_cells, uint32_t n_tiles) {
+  pos[0] = cv.take<float2>(nb);
+  pos[1] = cv.take<float2>(nb);
+  d.pos_old = cv.take<float2>(nb);
+  d.vel = cv.take<float2>(nb);
+  d.acc = cv.take<float2>(ns ? nb : 0);
+  d.rot = cv.take<float>(nb);
+  d.angvel = cv.take<float>(nb);
+  d.mass = cv.take<float>(nb);
+  d.inertia = cv.take<float>(nb);
+  d.gmod = cv.take<float>(nb);
+  d.bound_r = cv.take<float>(nb);
+  d.bflags = cv.take<uint8_t>(nb);
+  d.pend_acc = cv.take<float2>(nb);
+  d.pend_torque = cv.take<float>(nb);
+  d.vreq = cv.take<float2>(nb);
+  d.body_world = cv.take<uint32_t>(nb);
+  d.body_col_start = cv.take<uint32_t>(nb + 1);
+  d.body_cols = cv.take<uint32_t>(nc);
+  d.body_spr_start = cv.take<uint32_t>(nb + 1);
+  d.body_spr = cv.take<uint32_t>(2 * (size_t)ns);
+  d.col_parent = cv.take<uint32_t>(nc);
+  d.col_off = cv.take<float2>(nc);
+  d.col_radius = cv.take<float>(nc);
+  d.col_memb = cv.take<uint32_t>(nc);
+  d.col_filt = cv.take<uint32_t>(nc);
+  d.col_sensor = cv.take<uint8_t>(nc);
+  d.snap = cv.take<float2>(nc);
+  d.col_world = cv.take<uint32_t>(nc);
+  d.spr_a = cv.take<uint32_t>(ns);
+  d.spr_b = cv.take<uint32_t>(ns);
+  d.spr_rest = cv.take<float>(ns);
+  d.spr_k = cv.take<float>(ns);
+  d.spr_c = cv.take<float>(ns);
+  d.jnt_a = cv.take<uint32_t>(nj);
+  d.jnt_b = cv.take<uint32_t>(nj);
+  d.jnt_anchor_a = cv.take<float2>(nj);
+  d.jnt_anchor_b = cv.take<float2>(nj);
+  d.jnt_dist = cv.take<float>(nj);
+  d.jnt_target = cv.take<float>(nj);
+  d.circles = cv.take<float>(3 * (size_t)ncirc);
+  d.wparam = cv.take<WorldParam>(nw);
+  d.cell_count = cv.take<uint32_t>(n_cells);
+  d.cell_start = cv.take<uint32_t>((size_t)n_cells + 1);
+  d.rank = cv.take<uint32_t>(nc);
+  d.sorted = cv.take<float4>(nc);
+  d.tile_state = cv.take<unsigned long long>(n_tiles);
+  *counters = cv.take<Counters>(1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// substep / step orchestration
+// ---------------------------------------------------------------------------
+namespace {
+
+enum { PHASE_SCAN = 0, PHASE_SCATTER = 1, PHASE_CONTACT = 2, PHASE_JOINTS = 3, PHASE_INTEGRATE = 4, N_PHASES = 5 };
+
+void mark_begin(blobs_world* w, int phase) {
+  if (!w->recording) return;
+  TimingSet::Mark m{phase, nullptr, nullptr};
+  cudaEventCreate(&m.a);
+  cudaEventCreate(&m.b);
+  if (w->capturing) cudaEventRecordWithFlags(m.a, w->st(), cudaEventRecordExternal);
+  else cudaEventRecord(m.a, w->st());
+  w->recording->marks.push_back(m);
+}
+
+void mark_end(blobs_world* w) {
+  if (!w->recording) return;
+  cudaEvent_t b = w->recording->marks.back().b;
+  if (w->capturing) cudaEventRecordWithFlags(b, w->st(), cudaEventRecordExternal);
+  else cudaEventRecord(b, w->st());
+}
+
+void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
+  const WorldDev& d = w->dev;
+  float2* in = w->pos[w->cur];
+  float2* out = w->pos[w->cur ^ 1u];
+  const bool coll = w->cfg.collisions_enabled && w->nc > 0;
+  cudaStream_t st = w->st();
+  const uint64_t n_colours = w->colour_offsets.empty() ? 0 : w->colour_offsets.size() - 1;
+  auto joints = [&](float2* p) {
+    mark_begin(w, PHASE_JOINTS);
+    for (uint32_t it = 0; it < w->cfg.joint_iterations; ++it)
+      for (size_t k = 0; k < n_colours; ++k) launch_joints(d, p, w->colour_offsets[k], w->colour_offsets[k + 1], dt, st);
+    mark_end(w);
+    w->enqueued += (uint64_t)w->cfg.joint_iterations * n_colours;
+  };
+  if (coll && !w->keys_valid) {
+    launch_keys(d, w->multiworld, st);
+    w->enqueued += 1;
+  }
+  if (coll) {
+    mark_begin(w, PHASE_SCAN);
+    launch_scan(d, st);
+    mark_end(w);
+    w->enqueued += 1;
+  }
+  if (coll || w->has_springs) {
+    mark_begin(w, PHASE_SCATTER);
+    launch_scatter_forces(d, in, w->multiworld, coll, w->has_springs, pending, st);
+    mark_end(w);
+    w->enqueued += 1;
+  }
+  if (coll) {
+    const bool fuse = !w->has_joints;
+    mark_begin(w, PHASE_CONTACT);
+    launch_contacts(d, in, out, w->multiworld, w->single, w->has_springs, pending, fuse, dt, old_dt, true,
+                    w->rot_dynamic, st);
+    mark_end(w);
+    w->enqueued += 1;
+    if (!fuse) {
+      joints(out);
+      mark_begin(w, PHASE_INTEGRATE);
+      launch_integrate(d, out, out, w->multiworld, w->single, w->has_springs, pending, dt, old_dt, true,
+                       w->rot_dynamic, st);
+      mark_end(w);
+      w->enqueued += 1;
+    }
+    w->keys_valid = true;
+  } else {
+    if (w->has_joints) joints(in);
+    mark_begin(w, PHASE_INTEGRATE);
+    launch_integrate(d, in, out, w->multiworld, w->single, w->has_springs, pending, dt, old_dt, false,
+                     w->rot_dynamic, st);
+    mark_end(w);
+    w->enqueued += 1;
+    w->keys_valid = false;
+  }
+  w->cur ^= 1u;
+}
+
+// One reference `integrate(substeps, delta)` (physics.rs:397-422) enqueued
+// eagerly, honouring pending requests and the old_dt ratio.
+void enqueue_integrate(blobs_world* w, float delta) {
+  const float step_delta = delta / (float)w->cfg.substeps;
+  for (uint32_t s = 0; s < w->cfg.substeps; ++s) {
+    enqueue_substep(w, step_delta, w->old_dt, w->pending);
+    w->pending = false;
+    if (w->any_dynamic) w->old_dt = step_delta;
+  }
+}
+
+uint32_t f2bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+}
+
+// `n_steps` steady-state steps (no pending request, old_dt == step delta)
+// from one cached CUDA graph.
+int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
+  const float step_delta = delta / (float)w->cfg.substeps;
+  const bool coll = w->cfg.collisions_enabled && w->nc > 0;
+  if (coll && !w->keys_valid) {
+    launch_keys(w->dev, w->multiworld, w->st());
+    w->keys_valid = true;
+  }
+  GraphKey key{f2bits(delta), w->cur, n_steps, w->timing ? 1u : 0u};
+  auto it = w->graphs.find(key);
+  const uint32_t cur0 = w->cur;
+  if (it == w->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(w->st(), cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return blobs_map_cuda(e);
+    w->capturing = true;
+    w->recording = w->timing ? &w->graph_timing[key] : nullptr;
+    const uint64_t before = w->enqueued;
+    for (uint32_t n = 0; n < n_steps; ++n)
+      for (uint32_t s = 0; s < w->cfg.substeps; ++s) enqueue_substep(w, step_delta, step_delta, false);
+    w->capturing = false;
+    w->recording = nullptr;
+    w->graph_kernels[key] = w->enqueued - before;
+    w->enqueued = before;
+    e = cudaStreamEndCapture(w->st(), &g);
+    if (e != cudaSuccess) return blobs_map_cuda(e);
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return blobs_map_cuda(e);
+    it = w->graphs.emplace(key, ge).first;
+    w->cur = cur0;  // capture did not execute anything
+  }
+  cudaError_t e = cudaGraphLaunch(it->second, w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  w->kernels_launched += w->graph_kernels[key];
+  if (w->timing) {
+    TimingSet* ts = &w->graph_timing[key];
+    if (std::find(w->launched_sets.begin(), w->launched_sets.end(), ts) == w->launched_sets.end())
+      w->launched_sets.push_back(ts);
+  }
+  w->cur = cur0 ^ ((n_steps * w->cfg.substeps) & 1u);
+  w->keys_valid = coll;
+  return BLOBS_OK;
+}
+
+int run_steps(blobs_world* w, double delta, uint32_t n_steps) {
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (!(delta > 0.0) || !std::isfinite(delta)) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  const float df = (float)delta;
+  const float step_delta = df / (float)w->cfg.substeps;
+  uint32_t done = 0;
+  // irregular first step: eager
+  while (done < n_steps && (w->pending || (w->any_dynamic && f2bits(w->old_dt) != f2bits(step_delta)))) {
+    if (w->timing) {
+      w->recording = &w->eager_timing;
+      if (std::find(w->launched_sets.begin(), w->launched_sets.end(), w->recording) == w->launched_sets.end())
+        w->launched_sets.push_back(w->recording);
+    }
+    const uint64_t before = w->enqueued;
+    enqueue_integrate(w, df);
+    w->kernels_launched += w->enqueued - before;
+    w->recording = nullptr;
+    w->time += delta;
+    ++done;
+  }
+  if (done < n_steps) {
+    int st = launch_steady(w, df, n_steps - done);
+    if (st) return st;
+    w->time += delta * (double)(n_steps - done);
+  }
+  e = cudaGetLastError();
+  return blobs_map_cuda(e);
+}
+
+int read_status(blobs_world* w) {
+  cudaError_t e = cudaMemcpyAsync(w->hcounters, w->dev.contacts_total, sizeof(Counters), cudaMemcpyDeviceToHost,
+                                  w->st());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  w->sticky_status |= w->hcounters->status;
+  if (w->sticky_status & ST_NAN) return BLOBS_ERR_NAN;
+  if (w->sticky_status & ST_TIMEOUT) return BLOBS_ERR_TIMEOUT;
+  if (w->sticky_status & ST_BAD_INDEX) return BLOBS_ERR_INVALID_ARGUMENT;
+  return BLOBS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// internal API shared with the other translation units
+// ---------------------------------------------------------------------------
+const WorldDev* blobs_world_dev(blobs_world* w) { return w && w->loaded ? &w->dev : nullptr; }
+cudaStream_t blobs_world_stream(blobs_world* w) { return w ? w->st() : nullptr; }
+float2* blobs_world_pos(blobs_world* w) { return w && w->loaded ? w->pos[w->cur] : nullptr; }
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int blobs_abi_version(void) { return BLOBS_ABI_VERSION; }
+
+void blobs_config_default(blobs_config* cfg) {
+  if (!cfg) return;
+  cfg->gravity[0] = 0.0f;
+  cfg->gravity[1] = 0.0f;
+  cfg->substeps = 8;
+  cfg->joint_iterations = 4;
+  cfg->collisions_enabled = 1;
+  cfg->cell_size = 0.0f;
+  cfg->device = 0;
+}
+
+const char* blobs_status_string(int status) {
+  switch (status) {
+    case BLOBS_OK: return "ok";
+    case BLOBS_ERR_INVALID_HANDLE: return "invalid handle";
+    case BLOBS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case BLOBS_ERR_OVERFLOW: return "capacity overflow";
+    case BLOBS_ERR_NAN: return "NaN in contact normal or rotation";
+    case BLOBS_ERR_CUDA: return "CUDA runtime error";
+    case BLOBS_ERR_TIMEOUT: return "device wait timed out";
+    case BLOBS_ERR_NO_DEVICE: return "no usable CUDA device";
+    case BLOBS_ERR_OUT_OF_MEMORY: return "device out of memory";
+    case BLOBS_ERR_STATE: return "invalid state for this call";
+    default: return "unknown status";
+  }
+}
+
+int blobs_world_create(const blobs_config* cfg, blobs_world** out) {
+  if (!out) return BLOBS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  blobs_config c;
+  if (cfg) c = *cfg;
+  else blobs_config_default(&c);
+  if (c.substeps == 0) return BLOBS_ERR_INVALID_ARGUMENT;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) return BLOBS_ERR_NO_DEVICE;
+  if (c.device < 0 || c.device >= count) return BLOBS_ERR_INVALID_ARGUMENT;
+  e = cudaSetDevice(c.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  blobs_world* w = new blobs_world();
+  w->cfg = c;
+  e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&w->hcounters), sizeof(Counters));
+  if (e != cudaSuccess) {
+    delete w;
+    return blobs_map_cuda(e);
+  }
+  *out = w;
+  return BLOBS_OK;
+}
+
+int blobs_world_destroy(blobs_world* w) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  cudaSetDevice(w->cfg.device);
+  if (w->stream) cudaStreamSynchronize(w->stream);
+  delete w;
+  return BLOBS_OK;
+}
+
+int blobs_world_set_config(blobs_world* w, const blobs_config* cfg) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!cfg || cfg->substeps == 0 || cfg->device != w->cfg.device) return BLOBS_ERR_INVALID_ARGUMENT;
+  const bool gravity_changed = cfg->gravity[0] != w->cfg.gravity[0] || cfg->gravity[1] != w->cfg.gravity[1];
+  const bool cs_changed = cfg->cell_size != w->cfg.cell_size;
+  w->cfg = *cfg;
+  w->dev.gravity = v2(cfg->gravity[0], cfg->gravity[1]);
+  w->drop_graphs();
+  (void)gravity_changed;
+  (void)cs_changed;
+  return BLOBS_OK;
+}
+
+int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!scene) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  HostScene h;
+  int st = build_host_scene(w->cfg, *scene, h);
+  if (st) return st;
+  cudaStreamSynchronize(w->st());
+  w->drop_graphs();
+  if (w->arena) cudaFree(w->arena);
+  w->arena = nullptr;
+  w->loaded = false;
+
+  const uint32_t nb = scene->n_bodies, nc = scene->n_colliders, ns = scene->n_springs, nj = scene->n_joints;
+  const uint32_t nw = scene->n_worlds ? scene->n_worlds : 1, ncirc = scene->n_circles;
+  const uint32_t n_tiles = (h.n_cells + SCAN_TILE - 1) / SCAN_TILE;
+  WorldDev d{};
+  Counters* counters = nullptr;
+  Carver sizer;
+  carve(sizer, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles);
+  e = cudaMalloc(&w->arena, sizer.off + 256);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  Carver cv;
+  cv.base = static_cast<char*>(w->arena);
+  carve(cv, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles);
+  d.n_bodies = nb;
+  d.n_cols = nc;
+  d.n_springs = ns;
+  d.n_joints = nj;
+  d.n_worlds = nw;
+  d.n_circles = ncirc;
+  d.n_cells = h.n_cells;
+  d.n_tiles = n_tiles;
+  d.gravity = v2(w->cfg.gravity[0], w->cfg.gravity[1]);
+  d.contacts_total = &counters->contacts_total;
+  d.pushouts_total = &counters->pushouts_total;
+  d.contacts_sub = &counters->contacts_sub;
+  d.status = &counters->status;
+  d.tile_counter = &counters->tile_counter;
+  w->dcounters = counters;
+
+  cudaStream_t s = w->stream;
+  e = cudaSuccess;
+#define UP(dst, src) \
+  if (e == cudaSuccess) e = up(dst, src, s)
+  UP(w->pos[0], h.pos);
+  UP(d.pos_old, h.pos_old);
+  UP(d.vel, h.vel);
+  UP(d.rot, h.rot);
+  UP(d.angvel, h.angvel);
+  UP(d.mass, h.mass);
+  UP(d.inertia, h.inertia);
+  UP(d.gmod, h.gmod);
+  UP(d.bound_r, h.bound_r);
+  UP(d.bflags, h.bflags);
+  UP(d.pend_acc, h.pend_acc);
+  UP(d.pend_torque, h.pend_torque);
+  UP(d.vreq, h.vreq);
+  UP(d.body_world, h.body_world);
+  UP(d.body_col_start, h.body_col_start);
+  UP(d.body_cols, h.body_cols);
+  UP(d.body_spr_start, h.body_spr_start);
+  UP(d.body_spr, h.body_spr);
+  UP(d.col_parent, h.col_parent);
+  UP(d.col_off, h.col_off);
+  UP(d.col_radius, h.col_radius);
+  UP(d.col_memb, h.col_memb);
+  UP(d.col_filt, h.col_filt);
+  UP(d.col_sensor, h.col_sensor);
+  UP(d.snap, h.snap);
+  UP(d.col_world, h.col_world);
+  UP(d.spr_a, h.spr_a);
+  UP(d.spr_b, h.spr_b);
+  UP(d.spr_rest, h.spr_rest);
+  UP(d.spr_k, h.spr_k);
+  UP(d.spr_c, h.spr_c);
+  UP(d.jnt_a, h.jnt_a);
+  UP(d.jnt_b, h.jnt_b);
+  UP(d.jnt_anchor_a, h.anchor_a);
+  UP(d.jnt_anchor_b, h.anchor_b);
+  UP(d.jnt_dist, h.jnt_dist);
+  UP(d.jnt_target, h.jnt_target);
+  UP(d.circles, h.circles);
+  UP(d.wparam, h.wparam);
+#undef UP
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)h.n_cells, s);
+  if (e == cudaSuccess && n_tiles) e = cudaMemsetAsync(d.tile_state, 0, sizeof(unsigned long long) * n_tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(Counters), s);
+  if (e != cudaSuccess) {
+    cudaFree(w->arena);
+    w->arena = nullptr;
+    return blobs_map_cuda(e);
+  }
+  w->dev = d;
+  w->nb = nb;
+  w->nc = nc;
+  w->ns = ns;
+  w->nj = nj;
+  w->nw = nw;
+  w->ncirc = ncirc;
+  w->multiworld = nw > 1;
+  w->single = h.single;
+  w->has_springs = ns > 0;
+  w->has_joints = nj > 0;
+  w->rot_dynamic = h.rot_dynamic;
+  w->any_dynamic = h.any_dynamic;
+  w->pending = h.pending;
+  w->keys_valid = false;
+  w->colour_offsets = h.colour_offsets;
+  w->joint_order = h.joint_order;
+  w->old_dt = old_dt;
+  w->time = 0.0;
+  w->accumulator = 0.0;
+  w->cur = 0;
+  w->sticky_status = 0;
+  w->loaded = true;
+  e = cudaStreamSynchronize(s);  // host vectors die at return
+  return blobs_map_cuda(e);
+}
+
+int blobs_world_step(blobs_world* w, double delta) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  return run_steps(w, delta, 1);
+}
+
+int blobs_world_rollout(blobs_world* w, double delta, uint32_t n_steps) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (n_steps == 0) return BLOBS_OK;
+  return run_steps(w, delta, n_steps);
+}
+
+int blobs_world_fixed_step(blobs_world* w, double frame_time) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  // physics.rs:84-99
+  w->accumulator += frame_time;
+  const double delta = 1.0 / 60.0;
+  int max_steps = 3;
+  while (w->accumulator >= delta && max_steps > 0) {
+    int st = run_steps(w, delta, 1);
+    if (st) return st;
+    w->accumulator -= delta;
+    max_steps -= 1;
+  }
+  return BLOBS_OK;
+}
+
+int blobs_world_sync(blobs_world* w) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_OK;
+  cudaSetDevice(w->cfg.device);
+  return read_status(w);
+}
+
+int blobs_world_read_bodies(blobs_world* w, float* pos, float* pos_old, float* vel, float* rotation, float* angvel) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaSetDevice(w->cfg.device);
+  const size_t n = w->nb;
+  cudaError_t e = cudaSuccess;
+  cudaStream_t s = w->st();
+  if (pos && n) e = cudaMemcpyAsync(pos, w->pos[w->cur], n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && pos_old && n) e = cudaMemcpyAsync(pos_old, w->dev.pos_old, n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && vel && n) e = cudaMemcpyAsync(vel, w->dev.vel, n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && rotation && n) e = cudaMemcpyAsync(rotation, w->dev.rot, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && angvel && n) e = cudaMemcpyAsync(angvel, w->dev.angvel, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  return read_status(w);
+}
+
+int blobs_world_read_snapshots(blobs_world* w, float* xy) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (!xy) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  cudaError_t e = cudaSuccess;
+  if (w->nc) e = cudaMemcpyAsync(xy, w->dev.snap, (size_t)w->nc * 8, cudaMemcpyDeviceToHost, w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  return read_status(w);
+}
+
+int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_substep) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaSetDevice(w->cfg.device);
+  int st = read_status(w);
+  if (total) *total = w->hcounters->contacts_total;
+  if (last_substep) *last_substep = w->hcounters->contacts_sub;
+  return st;
+}
+
+int blobs_world_pushout_count(blobs_world* w, uint64_t* total) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaSetDevice(w->cfg.device);
+  int st = read_status(w);
+  if (total) *total = w->hcounters->pushouts_total;
+  return st;
+}
+
+int blobs_world_time(blobs_world* w, double* time, double* accumulator) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (time) *time = w->time;
+  if (accumulator) *accumulator = w->accumulator;
+  return BLOBS_OK;
+}
+
+int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (order && !w->joint_order.empty())
+    std::memcpy(order, w->joint_order.data(), w->joint_order.size() * sizeof(uint32_t));
+  if (n_colours) *n_colours = w->colour_offsets.empty() ? 0u : (uint32_t)(w->colour_offsets.size() - 1);
+  return BLOBS_OK;
+}
+
+int blobs_world_set_stream(blobs_world* w, void* stream) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  // the legacy / per-thread default streams cannot be captured into graphs
+  if (stream == (void*)cudaStreamLegacy || stream == (void*)cudaStreamPerThread) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  cudaError_t e = cudaStreamSynchronize(w->st());
+  w->user_stream = static_cast<cudaStream_t>(stream);
+  return blobs_map_cuda(e);
+}
+
+int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_old, const float* vel,
+                             const float* rotation, const float* angvel) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaSetDevice(w->cfg.device);
+  const size_t n = w->nb;
+  cudaStream_t s = w->st();
+  cudaError_t e = cudaSuccess;
+  if (pos && n) e = cudaMemcpyAsync(w->pos[w->cur], pos, n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && pos_old && n) e = cudaMemcpyAsync(w->dev.pos_old, pos_old, n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && vel && n) e = cudaMemcpyAsync(w->dev.vel, vel, n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && rotation && n) e = cudaMemcpyAsync(w->dev.rot, rotation, n * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && angvel && n) {
+    e = cudaMemcpyAsync(w->dev.angvel, angvel, n * 4, cudaMemcpyHostToDevice, s);
+    if (!w->rot_dynamic) {  // a non-zero angular velocity needs the rotation update
+      for (size_t i = 0; i < n && !w->rot_dynamic; ++i) w->rot_dynamic = angvel[i] != 0.0f;
+      if (w->rot_dynamic) w->drop_graphs();
+    }
+  }
+  return blobs_map_cuda(e);
+}
+
+int blobs_world_kernel_launches(blobs_world* w, uint64_t* count) {
+  if (!w || !count) return BLOBS_ERR_INVALID_HANDLE;
+  *count = w->kernels_launched;
+  return BLOBS_OK;
+}
+
+int blobs_world_set_timing(blobs_world* w, int enabled) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  w->timing = enabled != 0;
+  return BLOBS_OK;
+}
+
+int blobs_world_phase_times(blobs_world* w, double* ms, uint64_t* launches, uint32_t n_phases) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!ms || !launches || n_phases < N_PHASES) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  cudaError_t e = cudaStreamSynchronize(w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  for (uint32_t p = 0; p < n_phases; ++p) ms[p] = 0.0, launches[p] = 0;
+  for (TimingSet* ts : w->launched_sets)
+    for (auto& m : ts->marks) {
+      float t = 0.0f;
+      if (cudaEventElapsedTime(&t, m.a, m.b) == cudaSuccess) {
+        ms[m.phase] += t;
+        launches[m.phase] += 1;
+      }
+    }
+  w->launched_sets.clear();
+  w->eager_timing.destroy();
+  return BLOBS_OK;
+}
+
+int blobs_body_mass_inertia(uint32_t n_bodies, uint32_t n_colliders, const uint32_t* col_parent,
+                            const float* col_offset, const float* col_radius, const float* col_mass_override,
+                            const uint8_t* col_sensor, float* mass_out, float* inertia_out) {
+  if (!mass_out || !inertia_out) return BLOBS_ERR_INVALID_ARGUMENT;
+  if (n_colliders && (!col_parent || !col_radius)) return BLOBS_ERR_INVALID_ARGUMENT;
+  std::vector<float> m(n_bodies, 0.0f), I(n_bodies, 0.0f);
+  std::vector<uint8_t> has(n_bodies, 0);
+  for (uint32_t c = 0; c < n_colliders; ++c)
+    if (col_parent[c] >= n_bodies) return BLOBS_ERR_INVALID_ARGUMENT;
+  // Each handle sits twice in the body's collider list (collider.rs:180 and
+  // physics.rs:144); the sum runs over that list in order.
+  for (uint32_t c = 0; c < n_colliders; ++c) {
+    const uint32_t b = col_parent[c];
+    has[b] = 1;
+    if (col_sensor && col_sensor[c]) continue;
+    const float r = col_radius[c];
+    const float cm = (col_mass_override && !std::isnan(col_mass_override[c])) ? col_mass_override[c] : r * 2.0f;
+    const float2 off = col_offset ? v2(col_offset[2 * c], col_offset[2 * c + 1]) : v2(0.0f, 0.0f);
+    const float d = len2(off);
+    float ci = 0.5f * cm * (r * r);
+    ci = ci + cm * (d * d);
+    for (int twice = 0; twice < 2; ++twice) {
+      m[b] = m[b] + cm;
+      I[b] = I[b] + ci;
+    }
+  }
+  for (uint32_t b = 0; b < n_bodies; ++b) {
+    if (!has[b]) {
+      mass_out[b] = 1.0f;  // RigidBodyBuilder::build default (rigid_body.rs:385,388)
+      inertia_out[b] = 1.0f;
+      continue;
+    }
+    mass_out[b] = m[b] == 0.0f ? 1.0f : m[b];
+    inertia_out[b] = I[b] == 0.0f ? 1.0f : I[b];
+  }
+  return BLOBS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,234 @@
+/*
+ * blobs_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the blobs
+ * per-step simulation path (darthdeus/blobs 0.2.1, blobs/src/physics.rs).
+ *
+ * This is the thin FFI layer that a host keeping the reference's `Physics`
+ * API (rigid-body / collider / spring / joint arenas, builders, handles)
+ * binds to: the host hands its arenas over as structure-of-arrays in arena
+ * iteration order, and `Physics::step(dt)` becomes `blobs_world_step`.
+ * The C++ mirror of that host API is include/blobs_physics.hpp.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (blobs_status).  They replace
+ *     the reference's panics: e.g. physics.rs:142 `expect` -> INVALID_HANDLE,
+ *     physics.rs:293 / :471-474 `assert!` -> NAN.
+ *   - Ownership: the world owns its device memory; all input arrays are host
+ *     memory, copied during the call; the caller keeps ownership.
+ *   - Threading: one world is driven by one host thread at a time (the
+ *     reference Physics is !Send: physics.rs:4 holds an Rc).  Each world owns
+ *     one CUDA stream; calls are asynchronous unless documented otherwise,
+ *     and device-side failures are reported by the next synchronising call
+ *     (a read, blobs_world_sync).
+ *   - Arena order: bodies, colliders, springs and joints are given in the
+ *     order the reference iterates its thunderdome arenas (ascending slot).
+ *     That order is semantic: it fixes the contact pair sequence
+ *     (physics.rs:244-249), the spring order (:406-408), the joint order
+ *     (:426) and which body sees the `old_dt` ratio first (:338-339).
+ *   - There is no CPU fallback: without a usable CUDA device the calls that
+ *     need one return BLOBS_ERR_NO_DEVICE.
+ */
+#ifndef BLOBS_GPU_H
+#define BLOBS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BLOBS_ABI_VERSION 1
+
+typedef enum blobs_status {
+  BLOBS_OK = 0,
+  BLOBS_ERR_INVALID_HANDLE = 1,   /* unknown world / handle (physics.rs:142 expect) */
+  BLOBS_ERR_INVALID_ARGUMENT = 2, /* bad sizes, indices, NULL where required */
+  BLOBS_ERR_OVERFLOW = 3,         /* a caller-provided capacity was too small */
+  BLOBS_ERR_NAN = 4,              /* NaN contact normal / non-finite rotation (physics.rs:293,471-474) */
+  BLOBS_ERR_CUDA = 5,             /* a CUDA runtime call failed */
+  BLOBS_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+  BLOBS_ERR_NO_DEVICE = 7,        /* no usable CUDA device */
+  BLOBS_ERR_OUT_OF_MEMORY = 8,    /* device allocation failed */
+  BLOBS_ERR_STATE = 9             /* call not valid in the world's current state */
+} blobs_status;
+
+/* Body types, RigidBodyType (blobs/src/rigid_body.rs:219-242).  Only Static
+ * changes the step: kinematic bodies integrate like dynamic ones, exactly as
+ * in the reference (which only ever tests is_static). */
+enum { BLOBS_DYNAMIC = 0, BLOBS_STATIC = 1, BLOBS_KINEMATIC_POSITION = 2, BLOBS_KINEMATIC_VELOCITY = 3 };
+
+typedef struct blobs_world blobs_world;
+
+/* Physics knobs (physics.rs:6-27) plus the broadphase cell size. */
+typedef struct blobs_config {
+  float gravity[2];            /* Physics.gravity */
+  uint32_t substeps;           /* physics.rs:46, default 8 */
+  uint32_t joint_iterations;   /* physics.rs:47, default 4 */
+  uint32_t collisions_enabled; /* physics.rs:27,62, default 1 */
+  float cell_size;             /* broadphase cell edge; 0 = 2 * max collider radius * (1 + 1/64) */
+  int32_t device;              /* CUDA device ordinal, default 0 */
+} blobs_config;
+
+/*
+ * A whole scene in arena order.  `n_worlds` independent worlds may be packed
+ * back to back (batched mode): world w owns bodies
+ * [world_body_offsets[w], world_body_offsets[w+1]) and likewise colliders,
+ * springs and joints; cross-world references are rejected.  With n_worlds <= 1
+ * the offset arrays may be NULL.  NULL optional arrays take the defaults in
+ * brackets, which are the RigidBodyBuilder / ColliderBuilder defaults
+ * (rigid_body.rs:303-318, collider.rs:212-224).
+ */
+typedef struct blobs_scene {
+  uint32_t n_worlds;
+  const uint32_t* world_body_offsets;     /* n_worlds + 1 */
+  const uint32_t* world_collider_offsets; /* n_worlds + 1 */
+  const uint32_t* world_spring_offsets;   /* n_worlds + 1 */
+  const uint32_t* world_joint_offsets;    /* n_worlds + 1 */
+  const float* world_box;                 /* 4 per world (lo.x, lo.y, hi.x, hi.y) or NULL: wall extension */
+
+  /* RigidBody fields (rigid_body.rs:42-74) */
+  uint32_t n_bodies;
+  const float* pos;          /* 2n  position */
+  const float* pos_old;      /* 2n  position_old [= pos] */
+  const float* acc;          /* 2n  acceleration [0] */
+  const float* vel;          /* 2n  calculated_velocity [0] */
+  const float* vreq;         /* 2n  velocity_request value */
+  const uint8_t* vreq_set;   /* n   velocity_request is Some [0] */
+  const uint8_t* body_type;  /* n   [DYNAMIC] */
+  const float* rotation;     /* n   [0] */
+  const float* angvel;       /* n   angular_velocity [0] */
+  const float* torque;       /* n   [0] */
+  const float* gravity_mod;  /* n   [1] */
+  const float* mass;         /* n   calculated_mass: required (see blobs_body_mass_inertia) */
+  const float* inertia;      /* n   required */
+
+  /* Collider fields (collider.rs:3-20); spheres only, offset = translation */
+  uint32_t n_colliders;
+  const uint32_t* col_parent;  /* c   dense body index (required) */
+  const float* col_offset;     /* 2c  offset.translation [0] */
+  const float* col_radius;     /* c   required */
+  const uint8_t* col_sensor;   /* c   flags.is_sensor [0] */
+  const uint32_t* col_memb;    /* c   collision_groups.memberships [ALL] */
+  const uint32_t* col_filt;    /* c   collision_groups.filter [ALL] */
+  const float* col_snap;       /* 2c  absolute_transform.translation [transform(body) * offset] */
+
+  /* Spring (springs.rs:16-22), arena order */
+  uint32_t n_springs;
+  const uint32_t* spr_a;
+  const uint32_t* spr_b;
+  const float* spr_rest;
+  const float* spr_k;
+  const float* spr_c;
+
+  /* FixedJoint (joints.rs:7-19), arena order */
+  uint32_t n_joints;
+  const uint32_t* jnt_a;
+  const uint32_t* jnt_b;
+  const float* jnt_anchor_a;  /* 2j */
+  const float* jnt_anchor_b;  /* 2j */
+  const float* jnt_distance;  /* j */
+  const float* jnt_target;    /* j  target_angle */
+
+  /* Circle constraints (lib.rs:189-193), applied to every world */
+  uint32_t n_circles;
+  const float* circles;  /* 3 per circle: x, y, radius */
+} blobs_scene;
+
+/* ---- configuration / lifetime --------------------------------------------- */
+
+/* Physics::new defaults (physics.rs:37-69): gravity (0,0), 8 substeps,
+ * 4 joint iterations, collisions enabled, automatic cell size, device 0. */
+void blobs_config_default(blobs_config* cfg);
+const char* blobs_status_string(int status);
+int blobs_abi_version(void);
+
+/* Physics::new (physics.rs:37-69). */
+int blobs_world_create(const blobs_config* cfg, blobs_world** out);
+/* Drop. Frees all device memory of the world. */
+int blobs_world_destroy(blobs_world* w);
+/* Replace the physics knobs (gravity, substeps, ...) between steps. */
+int blobs_world_set_config(blobs_world* w, const blobs_config* cfg);
+
+/* Upload a scene, replacing the previous one (Physics::reset, physics.rs:71-76,
+ * followed by the insert_* calls).  The world's `old_dt` is set to `old_dt`
+ * (1.0 for a fresh Physics, physics.rs:67). */
+int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt);
+
+/* ---- the step -------------------------------------------------------------- */
+
+/* Physics::step (physics.rs:78-82): `substeps` substeps of gravity, springs,
+ * contacts, fixed joints, Verlet integration and constraints on every world. */
+int blobs_world_step(blobs_world* w, double delta);
+/* `n_steps` calls of step(delta) issued as one CUDA-graph launch. */
+int blobs_world_rollout(blobs_world* w, double delta, uint32_t n_steps);
+/* Physics::fixed_step (physics.rs:84-99): accumulator with delta = 1/60 and at
+ * most 3 integrate calls per frame. */
+int blobs_world_fixed_step(blobs_world* w, double frame_time);
+/* Wait for the world's stream; returns the first device-side error, if any. */
+int blobs_world_sync(blobs_world* w);
+
+/* Run the world's work on the caller's CUDA stream (a cudaStream_t) instead of
+ * its own; NULL returns to the world's own stream.  Lets a host order the
+ * step with its own copies and kernels. */
+int blobs_world_set_stream(blobs_world* w, void* stream);
+
+/* ---- host writes between steps ----------------------------------------------- */
+
+/* Overwrite body state in arena order, as a host mutating rbd.position /
+ * position_old / calculated_velocity / rotation / angular_velocity through
+ * Physics::get_mut_rbd (physics.rs:109-111) would.  Collider snapshots are not
+ * touched, exactly like the reference (they refresh in update_objects).  Any
+ * pointer may be NULL; asynchronous on the world's stream. */
+int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_old, const float* vel,
+                             const float* rotation, const float* angvel);
+
+/* ---- per-phase device timing (profiling aid; no reference counterpart) ------ */
+
+/* Number of kernels this world has issued (eagerly or as nodes of a launched
+ * graph) since it was created. */
+int blobs_world_kernel_launches(blobs_world* w, uint64_t* count);
+
+/* When enabled, CUDA events are recorded around each kernel phase of every
+ * substep (inside the step graphs). */
+int blobs_world_set_timing(blobs_world* w, int enabled);
+/* Device milliseconds and launch counts per phase since the previous call:
+ * [0] cell scan, [1] scatter + forces, [2] contacts (+ fused integration),
+ * [3] fixed joints, [4] integration.  n_phases >= 5.  Synchronising. */
+int blobs_world_phase_times(blobs_world* w, double* ms, uint64_t* launches, uint32_t n_phases);
+
+/* ---- reads (synchronising) ------------------------------------------------- */
+
+/* Body state in arena order: position, position_old, calculated_velocity,
+ * rotation, angular_velocity.  Any pointer may be NULL. */
+int blobs_world_read_bodies(blobs_world* w, float* pos, float* pos_old, float* vel, float* rotation,
+                            float* angvel);
+/* Collider absolute translations (Physics::col_position, physics.rs:155-157). */
+int blobs_world_read_snapshots(blobs_world* w, float* xy);
+/* Contacts counted by the contact pass: total since load and in the last
+ * substep (the reference's perf counter "collisions", physics.rs:316). */
+int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_substep);
+/* Contacts resolved with the coincident-centre push-out branch
+ * (physics.rs:272-286) since load. */
+int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
+/* Physics.time and the accumulator of fixed_step. */
+int blobs_world_time(blobs_world* w, double* time, double* accumulator);
+/* The joint processing order the GPU schedule uses (graph colouring: joints
+ * sorted by colour, then by arena index).  `order` holds n_joints entries. */
+int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours);
+
+/* ---- host-side helpers (no device needed) ---------------------------------- */
+
+/* RigidBody::update_mass_and_inertia (rigid_body.rs:96-128) for every body,
+ * including the reference's double registration of each collider handle
+ * (collider.rs:180 and physics.rs:144): mass = sum over handles of
+ * (mass_override or 2r) counted twice, sensors skipped, 0 -> 1.
+ * col_mass_override: NaN means None; the array may be NULL. */
+int blobs_body_mass_inertia(uint32_t n_bodies, uint32_t n_colliders, const uint32_t* col_parent,
+                            const float* col_offset, const float* col_radius, const float* col_mass_override,
+                            const uint8_t* col_sensor, float* mass_out, float* inertia_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLOBS_GPU_H */

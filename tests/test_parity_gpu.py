@@ -1,0 +1,252 @@
+"""GPU parity of the step through the C ABI against the oracle.
+
+Bit-exact where the reference arithmetic is reproducible (every contact /
+spring / Verlet / constraint op is a separately rounded f32 op in the same
+order; no push-out, no sin/cos of a non-zero rotation, no atan2), otherwise
+within the stated tolerance of the f32 and f64 oracles.
+"""
+import numpy as np
+import pytest
+
+from blobs_gb300 import native, scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(scene, steps, dt=None, **kw):
+    dt = scene.dt if dt is None else dt
+    with native.World(scene, **kw) as w:
+        for _ in range(steps):
+            w.step(dt)
+        out = w.read_bodies()
+        out["snap"] = w.read_snapshots()
+        out["contacts"], out["contacts_last"] = w.contact_count()
+        out["pushouts"] = w.pushout_count()
+        out["joint_order"] = w.joint_order()[0] if scene.n_joints else None
+    return out
+
+
+def run_oracle(scene, steps, dt=None, precision=32, joint_order=None):
+    dt = scene.dt if dt is None else dt
+    w = oracle.OracleWorld(scene, precision, joint_order=joint_order)
+    assert w.step(dt, steps) == 0
+    out = w.bodies()
+    out["snap"] = w.snapshots()
+    out["contacts"] = w.contacts
+    out["pushouts"] = w.pushouts
+    return out
+
+
+def assert_exact(got, want, keys=("pos", "pos_old", "vel")):
+    for k in keys:
+        g = got[k].astype(np.float64)
+        bad = np.argwhere(g != want[k])
+        assert len(bad) == 0, "%s: %d entries differ, first %s: gpu %s oracle %s" % (
+            k, len(bad), bad[:3].tolist(), g[tuple(bad[0])], want[k][tuple(bad[0])])
+
+
+# ---- configuration 1: 1,000 spheres in a walled box -------------------------
+
+def test_config1_single_step_bit_exact():
+    s = scenes.config1()
+    got, want = run_gpu(s, 1), run_oracle(s, 1)
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+    assert got["contacts"] == want["contacts"]
+
+
+def test_config1_full_600_step_rollout_bit_exact():
+    """All 600 steps (4,800 substeps): a single differing bit anywhere would
+    grow chaotically, so equality at the end pins every substep."""
+    s = scenes.config1()
+    got, want = run_gpu(s, s.n_steps), run_oracle(s, s.n_steps)
+    assert want["pushouts"] == 0
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+    assert got["contacts"] == want["contacts"]
+
+
+def test_rollout_graph_equals_eager_steps():
+    s = scenes.config1(seed=11, n=500)
+    a = run_gpu(s, 40)
+    with native.World(s) as w:
+        w.step(s.dt)
+        w.rollout(s.dt, 39)
+        b = w.read_bodies()
+    assert_exact(b, {k: a[k].astype(np.float64) for k in ("pos", "pos_old", "vel")})
+
+
+def test_determinism_two_runs_bitwise_equal():
+    s = scenes.config2(seed=5, n=20000)
+    a, b = run_gpu(s, 5), run_gpu(s, 5)
+    for k in ("pos", "pos_old", "vel"):
+        assert np.array_equal(a[k], b[k])
+
+
+# ---- configuration 2 (scaled): dense overlapping spheres ---------------------
+
+@pytest.mark.parametrize("n", [4096, 30000])
+def test_config2_scaled_bit_exact(n):
+    s = scenes.config2(seed=2, n=n)
+    got, want = run_gpu(s, 3), run_oracle(s, 3)
+    assert want["pushouts"] == 0
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+    assert got["contacts"] == want["contacts"]
+
+
+def test_config2_f64_tolerance():
+    """Single step vs the f64 re-run: |dx| <= 1e-4 (1 + |x|) per component
+    (dense overlaps make the f32/f64 difference of one step ~1e-6 relative)."""
+    s = scenes.config2(seed=21, n=4096)
+    got, want = run_gpu(s, 1), run_oracle(s, 1, precision=64)
+    err = np.abs(got["pos"].astype(np.float64) - want["pos"])
+    assert np.all(err <= 1e-4 * (1.0 + np.abs(want["pos"]))), err.max()
+
+
+def test_literal_2000_box_bit_exact():
+    s = scenes.config2(seed=8, n=20000, literal_box=True)
+    got, want = run_gpu(s, 2), run_oracle(s, 2)
+    assert_exact(got, want)
+
+
+# ---- springs, static bodies, sensors, groups, multi-collider bodies ---------
+
+def test_springs_bit_exact():
+    rng = np.random.Generator(np.random.PCG64(44))
+    s = scenes.random_world(rng, 3000, 0.1, 0.3, 0.35, 1.0, spring_frac=0.3, k_range=(10.0, 1e4),
+                            c_range=(0.0, 2.0))
+    got, want = run_gpu(s, 10), run_oracle(s, 10)
+    assert_exact(got, want)
+
+
+def test_static_bodies_sensors_groups_bit_exact():
+    s = scenes.config2(seed=31, n=5000)
+    rng = np.random.Generator(np.random.PCG64(31))
+    s.body_type[rng.random(s.n_bodies) < 0.1] = scenes.STATIC
+    s.col_sensor[rng.random(s.n_colliders) < 0.05] = 1
+    s.col_memb = rng.choice(np.array([1, 2, 3, 0xFFFFFFFF], np.uint32), s.n_colliders)
+    s.col_filt = rng.choice(np.array([1, 2, 0xFFFFFFFF], np.uint32), s.n_colliders)
+    s.gravity_mod = rng.uniform(0.0, 2.0, s.n_bodies).astype(np.float32)
+    got, want = run_gpu(s, 4), run_oracle(s, 4)
+    assert_exact(got, want)
+    assert got["contacts"] == want["contacts"]
+
+
+def test_multi_collider_bodies_bit_exact():
+    """Config 3 layout without joints: rotation stays 0, so the snapshots
+    (rot(0) * offset + p) are exact and the merged per-body contact order is
+    the reference's (outer collider, inner collider) sequence."""
+    s = scenes.config3(seed=3, n=6000, n_joints=0, n_springs=2000, side=90.0)
+    s.jnt_a = s.jnt_a[:0]
+    got, want = run_gpu(s, 4), run_oracle(s, 4)
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+    assert got["contacts"] == want["contacts"]
+
+
+def test_circle_constraint_bit_exact():
+    s = scenes.config1(seed=12, n=400)
+    s.world_box = None
+    s.circles = np.array([[0.0, 0.0, 12.0]], np.float32)
+    got, want = run_gpu(s, 30), run_oracle(s, 30)
+    assert_exact(got, want)
+
+
+def test_collisions_disabled_bit_exact():
+    s = scenes.config1(seed=13, n=300)
+    s.collisions_enabled = False
+    got, want = run_gpu(s, 10), run_oracle(s, 10)
+    assert_exact(got, want)
+    assert got["contacts"] == 0
+
+
+# ---- joints: coloured Gauss-Seidel --------------------------------------------
+
+def test_joints_single_collider_positions_exact_in_gpu_order():
+    """Single-collider bodies: snapshots do not depend on rotation, so the
+    positions are bit-exact against the oracle run in the GPU's colour order;
+    rotations use CUDA atan2f (tolerance 1e-5 rad)."""
+    rng = np.random.Generator(np.random.PCG64(6))
+    s = scenes.random_world(rng, 4000, 0.1, 0.25, 0.2, 0.5)
+    near = scenes._pairs_within(s.pos, 1.0)
+    pick = np.sort(rng.choice(len(near), 1500, replace=False))
+    scenes.add_fixed_joints(s, near[pick, 0], near[pick, 1])
+    got = run_gpu(s, 3)
+    want = run_oracle(s, 3, joint_order=got["joint_order"])
+    assert_exact(got, want)
+    np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
+
+
+def test_config3_scaled_tolerance():
+    """Multi-collider bodies + joints + springs: rotation enters the snapshots
+    through sin/cos, so one step is compared within |dx| <= 1e-4 (1 + |x|)
+    against the oracle in the GPU joint order, and against the f64 oracle."""
+    s = scenes.config3(seed=3, n=6000, n_joints=1500, n_springs=3000, side=90.0)
+    got = run_gpu(s, 1)
+    for prec in (32, 64):
+        want = run_oracle(s, 1, precision=prec, joint_order=got["joint_order"])
+        err = np.abs(got["pos"].astype(np.float64) - want["pos"])
+        assert np.all(err <= 1e-4 * (1.0 + np.abs(want["pos"]))), (prec, err.max())
+
+
+# ---- batched worlds -----------------------------------------------------------
+
+def test_batched_worlds_bit_exact_per_world():
+    s = scenes.config4(seed=14, n_worlds=24, nmin=64, nmax=1024)
+    got = run_gpu(s, 5)
+    for w in range(s.n_worlds):
+        sub = scenes.unpack_world(s, w)
+        want = run_oracle(sub, 5)
+        b0, b1 = int(s.world_body_offsets[w]), int(s.world_body_offsets[w + 1])
+        assert_exact({k: got[k][b0:b1] for k in ("pos", "pos_old", "vel")}, want)
+
+
+# ---- known answers of the reference quirks on the GPU -------------------------
+
+def test_pushout_coincident_spheres_gpu():
+    s = scenes.spheres([[1, 1], [1, 1], [5, 5]], [0.5, 0.5, 0.2], gravity=(0, 0))
+    got, want = run_gpu(s, 1), run_oracle(s, 1)
+    assert got["pushouts"] == 1 == want["pushouts"]
+    assert_exact(got, want)
+
+
+def test_old_dt_ratio_changes_with_dt():
+    s = scenes.config1(seed=15, n=200)
+    with native.World(s) as w:
+        w.step(1 / 60)
+        w.step(1 / 60)
+        w.step(1 / 120)   # first dynamic body sees (1/960) / (1/480)
+        w.step(1 / 120)
+        got = w.read_bodies()
+    o = oracle.OracleWorld(s, 32)
+    o.step(1 / 60, 2)
+    o.step(1 / 120, 2)
+    assert_exact(got, o.bodies())
+
+
+def test_body_collider_transform_gpu():
+    """collider.rs:367-389 on the device: body at (2, 3) rotated pi/2, collider
+    offset (1, 1) -> absolute translation (1, 4)."""
+    s = scenes.empty_scene(1)
+    s.pos = np.array([[2.0, 3.0]], np.float32)
+    s.rotation = np.array([np.pi / 2], np.float32)
+    s.col_parent = np.zeros(1, np.uint32)
+    s.col_offset = np.array([[1.0, 1.0]], np.float32)
+    s.col_radius = np.array([0.5], np.float32)
+    s.col_mass_override = np.full(1, np.nan, np.float32)
+    s.col_sensor = np.zeros(1, np.uint8)
+    s.col_memb = np.full(1, scenes.ALL_GROUPS, np.uint32)
+    s.col_filt = np.full(1, scenes.ALL_GROUPS, np.uint32)
+    s.gravity = np.zeros(2, np.float32)
+    s.body_type = np.array([scenes.STATIC], np.uint8)
+    got = run_gpu(s, 1)
+    np.testing.assert_allclose(got["snap"][0], [1.0, 4.0], atol=1e-5)
+
+
+def test_fixed_step_accumulator():
+    s = scenes.config1(seed=16, n=100)
+    with native.World(s) as w:
+        w.fixed_step(0.05)        # 3 steps of 1/60 (max 3), accumulator 0
+        t, acc = w.time()
+        got = w.read_bodies()
+    assert abs(t - 3 / 60) < 1e-12 and abs(acc - (0.05 - 3 / 60)) < 1e-12
+    want = run_oracle(s, 3, dt=1 / 60)
+    assert_exact(got, want)
