@@ -282,7 +282,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded config2 generator: uniform positions with overlaps, N(0,0.5) velocities)",
-        "config": {"workload": "1M spheres, r~U[0.05,0.15], 40% packing (side %.1f, walled), g=(0,-9.81), "
+        "config": {"workload": "1M spheres, r~U[0.05,0.15], 40%% packing (side %.1f, walled), g=(0,-9.81), "
                                "dt=1/120, 8 substeps/step" % (float(scene.world_box[0, 2] * 2)),
                    "bodies": scene.n_bodies, "substeps": scene.substeps, "parallelism": "replicas" if world_size > 1
                    else "single", "l2": "flushed (256 MiB write) before every timed step",

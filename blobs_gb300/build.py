@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libblobs_gb300.so")
-SOURCES = ["kernels.cu", "world.cu"]
+SOURCES = ["kernels.cu", "single.cu", "world.cu", "physics.cpp"]
 HEADERS = ["device.cuh", "kernels.h", "world.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -38,12 +38,12 @@ def _newest(paths):
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    inc = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(HERE, "..", "include", "blobs_gpu.h")]
+    inc = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(HERE, "..", "include", x) for x in ("blobs_gpu.h", "blobs_physics.hpp")]
     objs = []
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or not os.path.exists(o) or os.path.getmtime(o) < _newest([s] + inc + [__file__]):
             jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])

@@ -35,7 +35,8 @@ struct WorldParam {
   float cs;             // cell edge
   float box_lo_x, box_lo_y, box_hi_x, box_hi_y;
   uint32_t has_box;     // axis-aligned wall extension enabled
-  uint32_t pad[3];
+  float inv_cs;         // 1 / cs (rounded once, on the host)
+  uint32_t pad[2];
 };
 
 // Every device pointer of a loaded scene.  Passed to kernels by value.
@@ -96,10 +97,18 @@ struct WorldDev {
   uint32_t* cell_start;      // n_cells + 1
   uint32_t* rank;            // per collider: slot inside its cell
   float4* sorted;            // per slot: (x, y, radius, collider index bits)
-  unsigned long long* tile_state;
-  uint32_t* tile_counter;
+  uint32_t* tile_sums;       // per scan tile
 
-  // counters
+  // single-sphere path: cell-sorted body storage, double-buffered
+  float4* sa[2];             // (snapshot x, y, radius, arena id bits)
+  float4* sb[2];             // (position x, y, position_old x, y)
+  float2* sv[2];             // calculated_velocity
+  float4* body_c;            // arena order: (mass, gravity_mod, bounding radius, flags | world << 8)
+  uint32_t* key;             // per storage slot: cell of the snapshot for the next substep
+  uint32_t* ckey;            // per storage slot: cell the permute sorted the body into
+  uint32_t* where;           // arena id -> storage slot
+
+  // counters, each spread over COUNTER_BINS bins that the host sums
   unsigned long long* contacts_total;
   unsigned long long* pushouts_total;
   uint32_t* contacts_sub;    // contacts of the most recent substep
@@ -128,10 +137,21 @@ __device__ __host__ __forceinline__ int32_t cell_coord(float v, float cs) {
   return (int32_t)q;
 }
 
+// Cell coordinate of the broadphase grid: floor(v * (1/cs)), saturating,
+// NaN -> 0.  Monotone in v; with cs >= 2 rmax (1 + 1/64) two spheres in
+// contact always land in 3x3-neighbouring cells for |v| / cs up to ~1e5.
+__device__ __host__ __forceinline__ int32_t grid_coord(float v, float inv_cs) {
+  float q = floorf(v * inv_cs);
+  if (q != q) return 0;
+  if (q >= 2147483648.0f) return 2147483647;
+  if (q <= -2147483648.0f) return (-2147483647 - 1);
+  return (int32_t)q;
+}
+
 // Global cell index of a point in world `wp`'s toroidal grid.
 __device__ __host__ __forceinline__ uint32_t cell_key(const WorldParam& wp, float2 s) {
-  uint32_t ix = (uint32_t)cell_coord(s.x, wp.cs) & ((1u << wp.log2w) - 1u);
-  uint32_t iy = (uint32_t)cell_coord(s.y, wp.cs) & ((1u << wp.log2h) - 1u);
+  uint32_t ix = (uint32_t)grid_coord(s.x, wp.inv_cs) & ((1u << wp.log2w) - 1u);
+  uint32_t iy = (uint32_t)grid_coord(s.y, wp.inv_cs) & ((1u << wp.log2h) - 1u);
   return wp.cell_base + ((iy << wp.log2w) | ix);
 }
 
@@ -144,10 +164,20 @@ __device__ __forceinline__ float2 collider_translation(float rot, float2 pos, fl
   return add(m, pos);
 }
 
+// Per-substep scalars of the integration.
+struct SubstepArgs {
+  float dt;
+  float old_dt;
+  float ratio_first;     // dt / old_dt, the first non-static body's factor (physics.rs:338)
+  float ratio_rest;      // dt / dt (exactly 1 for a finite non-zero dt)
+  uint32_t do_keys;
+  uint32_t rot_dynamic;  // 0: every angular velocity is 0 and no torque is pending -> rotation is constant
+};
+
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr uint32_t SPIN_LIMIT = 1u << 22;  // bounded waits: polls before giving up
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
+constexpr uint32_t COUNTER_BINS = 64;
 
 }  // namespace blobs

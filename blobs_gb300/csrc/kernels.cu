@@ -30,66 +30,89 @@ __device__ __forceinline__ WorldParam load_wparam(const WorldDev& w, uint32_t wo
   return w.wparam[world];
 }
 
-__device__ __forceinline__ void publish_tile(unsigned long long* ts, uint32_t tile, uint32_t flag, uint32_t value) {
-  unsigned long long v = ((unsigned long long)flag << 32) | value;
-  __threadfence();
-  *reinterpret_cast<volatile unsigned long long*>(ts + tile) = v;
-}
 
 // ---------------------------------------------------------------------------
-// k_cell_scan: cell_start[k] = sum(cell_count[0..k)), cell_start[n] = total,
-// cell_count[:] = 0.  Tiles are taken in launch order from a counter, so the
-// look-back only waits on tiles that are already running; the wait is bounded
-// (SPIN_LIMIT polls) and sets ST_TIMEOUT instead of hanging.
+// Cell scan in two wait-free kernels: k_tile_sums reduces each tile of
+// SCAN_TILE cell counts; k_scan_apply gives every tile its prefix by summing
+// the sums of all earlier tiles (at most a few thousand), then writes
+// cell_start[k] = sum(cell_count[0..k)), cell_start[n] = total, and resets
+// cell_count to zero for the next substep.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(SCAN_THREADS) k_cell_scan(WorldDev w) {
-  __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_prefix;
-  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(w.tile_counter, 1u);
-    if (s_tile == 0) *w.contacts_sub = 0u;
-  }
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_warp) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) s_warp[warp] = v;
   __syncthreads();
-  const uint32_t tile = s_tile;
-  if (tile >= w.n_tiles) {  // counter not reset: never index past tile_state
-    if (threadIdx.x == 0) set_status(w, ST_BAD_INDEX);
-    return;
+  uint32_t t = 0;
+  if (warp == 0) {
+    t = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
   }
+  return t;  // valid in warp 0
+}
+
+__device__ __forceinline__ void load_tile(const WorldDev& w, size_t base, uint32_t* v, bool zero) {
   const uint32_t n = w.n_cells;
-  const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
-  uint32_t v[SCAN_ITEMS];
-  const bool full = base + SCAN_ITEMS <= n;
-  if (full) {
+  if (base + SCAN_ITEMS <= n) {
     uint4* src = reinterpret_cast<uint4*>(w.cell_count + base);
 #pragma unroll
     for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
-      uint4 t = src[q];
+      const uint4 t = src[q];
       v[4 * q + 0] = t.x;
       v[4 * q + 1] = t.y;
       v[4 * q + 2] = t.z;
       v[4 * q + 3] = t.w;
-      src[q] = make_uint4(0u, 0u, 0u, 0u);
+      if (zero) src[q] = make_uint4(0u, 0u, 0u, 0u);
     }
   } else {
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-      size_t k = base + i;
+      const size_t k = base + i;
       v[i] = k < n ? w.cell_count[k] : 0u;
-      if (k < n) w.cell_count[k] = 0u;
+      if (zero && k < n) w.cell_count[k] = 0u;
     }
   }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(WorldDev w) {
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  load_tile(w, base, v, false);
+  uint32_t t = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) t += v[i];
+  t = block_sum(t, s_warp);
+  if (threadIdx.x == 0) w.tile_sums[blockIdx.x] = t;
+  if (blockIdx.x == 0 && threadIdx.x < COUNTER_BINS) w.contacts_sub[threadIdx.x] = 0u;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(WorldDev w) {
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_prefix;
+  // prefix of this tile = sum of the sums of tiles [0, blockIdx.x)
+  uint32_t p = 0;
+  for (uint32_t t = threadIdx.x; t < blockIdx.x; t += SCAN_THREADS) p += w.tile_sums[t];
+  p = block_sum(p, s_warp);
+  if (threadIdx.x == 0) s_prefix = p;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  load_tile(w, base, v, true);
   uint32_t tsum = 0;
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) tsum += v[i];
-
+  // exclusive scan of the thread sums across the block
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t x = tsum;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= (uint32_t)o) x += y;
   }
+  __syncthreads();  // s_warp reuse
   if (lane == 31) s_warp[warp] = x;
   __syncthreads();
   if (warp == 0) {
@@ -97,45 +120,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_cell_scan(WorldDev w) {
     uint32_t t = lane < NW ? s_warp[lane] : 0u;
 #pragma unroll
     for (int o = 1; o < NW; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
       if (lane >= (uint32_t)o) t += y;
     }
     if (lane < NW) s_warp[lane] = t;
   }
   __syncthreads();
-  const uint32_t thread_excl = (warp ? s_warp[warp - 1] : 0u) + x - tsum;
-  const uint32_t block_total = s_warp[SCAN_THREADS / 32 - 1];
-
-  if (threadIdx.x == 0) {
-    uint32_t excl = 0;
-    if (tile == 0) {
-      publish_tile(w.tile_state, 0, 2u, block_total);
-    } else {
-      publish_tile(w.tile_state, tile, 1u, block_total);
-      int64_t t = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      while (t >= 0) {
-        unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(w.tile_state + t);
-        uint32_t flag = (uint32_t)(st >> 32);
-        if (flag == 0u) {
-          if (++spins >= SPIN_LIMIT) {
-            set_status(w, ST_TIMEOUT);
-            break;
-          }
-          __nanosleep(32);
-          continue;
-        }
-        excl += (uint32_t)st;
-        if (flag == 2u) break;
-        --t;
-      }
-      publish_tile(w.tile_state, tile, 2u, excl + block_total);
-    }
-    s_prefix = excl;
-  }
-  __syncthreads();
-  uint32_t run = s_prefix + thread_excl;
-  if (full) {
+  uint32_t run = s_prefix + (warp ? s_warp[warp - 1] : 0u) + x - tsum;
+  const uint32_t n = w.n_cells;
+  if (base + SCAN_ITEMS <= n) {
     uint4* dst = reinterpret_cast<uint4*>(w.cell_start + base);
 #pragma unroll
     for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
@@ -150,7 +143,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_cell_scan(WorldDev w) {
   } else {
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-      size_t k = base + i;
+      const size_t k = base + i;
       if (k < n) {
         w.cell_start[k] = run;
         run += v[i];
@@ -195,10 +188,6 @@ template <bool MW, bool SCATTER, bool SPR, bool PEND>
 __global__ void __launch_bounds__(256) k_scatter_forces(WorldDev w, const float2* __restrict__ pos) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (SCATTER) {
-    if (blockIdx.x == 0) {
-      for (uint32_t t = threadIdx.x; t < w.n_tiles; t += blockDim.x) w.tile_state[t] = 0ull;
-      if (threadIdx.x == 0) *w.tile_counter = 0u;
-    }
     if (i < w.n_cols) {
       const float2 s = w.snap[i];
       const WorldParam wp = load_wparam(w, MW ? w.col_world[i] : 0u);
@@ -220,13 +209,6 @@ __global__ void __launch_bounds__(256) k_scatter_forces(WorldDev w, const float2
 // constraints (the reference refreshes them inside update_objects only), and
 // their cell keys/ranks for the next substep are recorded here.
 // ---------------------------------------------------------------------------
-struct SubstepArgs {
-  float dt;
-  float old_dt;
-  uint32_t do_keys;
-  uint32_t rot_dynamic;  // 0: every angular velocity is 0 and no torque is pending -> rotation is constant
-};
-
 template <bool MW, bool SPR, bool PEND, bool SINGLE>
 __device__ __forceinline__ void integrate_body(const WorldDev& w, uint32_t b, float2 p, float2* __restrict__ pos_out,
                                                const SubstepArgs& a) {
@@ -303,7 +285,7 @@ __device__ __forceinline__ void integrate_body(const WorldDev& w, uint32_t b, fl
 template <class F>
 __device__ __forceinline__ void for_each_candidate(const WorldDev& w, const WorldParam& wp, float2 s, F&& f) {
   const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
-  const uint32_t ix = (uint32_t)cell_coord(s.x, wp.cs), iy = (uint32_t)cell_coord(s.y, wp.cs);
+  const uint32_t ix = (uint32_t)grid_coord(s.x, wp.inv_cs), iy = (uint32_t)grid_coord(s.y, wp.inv_cs);
   const uint32_t x0 = (ix - 1u) & wm, x2 = (ix + 1u) & wm;
 #pragma unroll 1
   for (int oy = -1; oy <= 1; ++oy) {
@@ -398,19 +380,35 @@ __device__ __forceinline__ unsigned long long pair_key(uint32_t c, uint32_t c2) 
   return ((unsigned long long)hi << 33) | ((unsigned long long)lo << 1);
 }
 
+// Block-level sum of the contact / push-out counts, then one atomic per
+// block into one of COUNTER_BINS bins (spreads same-address atomics over L2
+// slices; the host sums the bins).  Every thread of the block must call it.
 __device__ __forceinline__ void count_contacts(const WorldDev& w, uint32_t ncontacts, uint32_t npush) {
-  const uint32_t lane = threadIdx.x & 31u;
+  __shared__ uint32_t s_c, s_p;
+  if (threadIdx.x == 0) {
+    s_c = 0u;
+    s_p = 0u;
+  }
+  __syncthreads();
   uint32_t t = ncontacts, p = npush;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     t += __shfl_down_sync(0xffffffffu, t, o);
     p += __shfl_down_sync(0xffffffffu, p, o);
   }
-  if (lane == 0 && t) {
-    atomicAdd(w.contacts_total, (unsigned long long)t);
-    atomicAdd(w.contacts_sub, t);
+  if ((threadIdx.x & 31u) == 0) {
+    if (t) atomicAdd(&s_c, t);
+    if (p) atomicAdd(&s_p, p);
   }
-  if (lane == 0 && p) atomicAdd(w.pushouts_total, (unsigned long long)p);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t bin = blockIdx.x & (COUNTER_BINS - 1);
+    if (s_c) {
+      atomicAdd(w.contacts_total + bin, (unsigned long long)s_c);
+      atomicAdd(w.contacts_sub + bin, s_c);
+    }
+    if (s_p) atomicAdd(w.pushouts_total + bin, (unsigned long long)s_p);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -671,6 +669,46 @@ __global__ void __launch_bounds__(256) k_keys(WorldDev w) {
 }
 
 // ---------------------------------------------------------------------------
+// k_emit_pairs: the broadphase output itself.  For every collider (one
+// thread per cell-sorted slot) and every candidate in its 3x3 cells with a
+// lower collider index, append (hi, lo) -- all candidates (mode 0) or only
+// pairs in contact after the reference's filters (mode 1: different parent,
+// groups test, dist < ra + rb, physics.rs:249-269).  Pairs past `cap` are
+// counted, not written.
+// ---------------------------------------------------------------------------
+template <bool MW>
+__global__ void __launch_bounds__(256) k_emit_pairs(WorldDev w, uint32_t mode, uint32_t* __restrict__ out,
+                                                    unsigned long long cap, unsigned long long* __restrict__ count) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= w.n_cols) return;
+  const float4 me = w.sorted[e];
+  const uint32_t c = __float_as_uint(me.w);
+  if (c >= w.n_cols) {
+    set_status(w, ST_BAD_INDEX);
+    return;
+  }
+  const float2 s = v2(me.x, me.y);
+  const WorldParam wp = load_wparam(w, MW ? w.col_world[c] : 0u);
+  for_each_candidate(w, wp, s, [&](uint32_t q) {
+    const float4 o = w.sorted[q];
+    const uint32_t c2 = __float_as_uint(o.w);
+    if (c2 >= c) return;
+    if (mode == 1u) {
+      if (w.col_parent[c2] == w.col_parent[c]) return;
+      const uint32_t m1 = w.col_memb[c], f1 = w.col_filt[c], m2 = w.col_memb[c2], f2 = w.col_filt[c2];
+      if (!((m1 & f2) != 0u && (m2 & f1) != 0u)) return;
+      const float2 axis = sub(s, v2(o.x, o.y));
+      if (!(len2(axis) < (me.z + o.z))) return;
+    }
+    const unsigned long long k = atomicAdd(count, 1ull);
+    if (k < cap) {
+      out[2 * k] = c;
+      out[2 * k + 1] = c2;
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
 static inline uint32_t blocks_for(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
@@ -684,7 +722,8 @@ void launch_keys(const WorldDev& w, bool mw, cudaStream_t st) {
 
 void launch_scan(const WorldDev& w, cudaStream_t st) {
   const uint32_t tiles = blocks_for(w.n_cells, SCAN_TILE);
-  k_cell_scan<<<tiles, SCAN_THREADS, 0, st>>>(w);
+  k_tile_sums<<<tiles, SCAN_THREADS, 0, st>>>(w);
+  k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(w);
 }
 
 #define BLOBS_DISPATCH_BOOL(v, NAME, ...) \
@@ -711,7 +750,7 @@ void launch_scatter_forces(const WorldDev& w, const float2* pos, bool mw, bool s
 void launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
                      bool pending, bool fuse, float dt, float old_dt, bool do_keys, bool rot_dynamic,
                      cudaStream_t st) {
-  SubstepArgs a{dt, old_dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
+  SubstepArgs a{dt, old_dt, dt / old_dt, dt / dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
   if (single) {
     if (!w.n_cols) return;
     const uint32_t g = blocks_for(w.n_cols, 256);
@@ -737,12 +776,20 @@ void launch_joints(const WorldDev& w, float2* pos, uint32_t j0, uint32_t j1, flo
 void launch_integrate(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
                       bool pending, float dt, float old_dt, bool do_keys, bool rot_dynamic, cudaStream_t st) {
   if (!w.n_bodies) return;
-  SubstepArgs a{dt, old_dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
+  SubstepArgs a{dt, old_dt, dt / old_dt, dt / dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
   const uint32_t g = blocks_for(w.n_bodies, 256);
   BLOBS_DISPATCH_BOOL(mw, MW,
     BLOBS_DISPATCH_BOOL(springs, SP,
       BLOBS_DISPATCH_BOOL(pending, PE,
         BLOBS_DISPATCH_BOOL(single, SI, k_integrate<MW, SP, PE, SI><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+}
+
+void launch_emit_pairs(const WorldDev& w, bool mw, uint32_t mode, uint32_t* out, unsigned long long cap,
+                       unsigned long long* count, cudaStream_t st) {
+  if (!w.n_cols) return;
+  const uint32_t g = blocks_for(w.n_cols, 256);
+  if (mw) k_emit_pairs<true><<<g, 256, 0, st>>>(w, mode, out, cap, count);
+  else k_emit_pairs<false><<<g, 256, 0, st>>>(w, mode, out, cap, count);
 }
 
 }  // namespace blobs

@@ -21,12 +21,26 @@ using namespace blobs;
 namespace {
 
 struct Counters {
-  unsigned long long contacts_total;
-  unsigned long long pushouts_total;
-  uint32_t contacts_sub;
+  unsigned long long contacts_total[COUNTER_BINS];
+  unsigned long long pushouts_total[COUNTER_BINS];
+  uint32_t contacts_sub[COUNTER_BINS];
   uint32_t status;
-  uint32_t tile_counter;
-  uint32_t pad;
+  uint32_t pad[3];
+  unsigned long long contacts() const {
+    unsigned long long t = 0;
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += contacts_total[i];
+    return t;
+  }
+  unsigned long long pushouts() const {
+    unsigned long long t = 0;
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += pushouts_total[i];
+    return t;
+  }
+  unsigned long long sub() const {
+    unsigned long long t = 0;
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += contacts_sub[i];
+    return t;
+  }
 };
 
 inline uint32_t next_pow2(uint64_t v) {
@@ -99,6 +113,8 @@ struct blobs_world {
   uint32_t nb = 0, nc = 0, ns = 0, nj = 0, nw = 0, ncirc = 0;
   bool multiworld = false, single = false, has_springs = false, has_joints = false, rot_dynamic = false;
   bool any_dynamic = false;
+  bool sorted_storage = false;  // single-sphere path: body state in cell-sorted storage (single.cu)
+  float v_div = 0.0f;           // sorted storage without springs: V holds disp of a substep of this dt
   bool pending = false;
   bool keys_valid = false;
   std::vector<uint32_t> colour_offsets;  // colour k = joints [colour_offsets[k], colour_offsets[k+1]) in processing order
@@ -418,6 +434,7 @@ int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h
     wp.log2w = ilog2(W);
     wp.log2h = ilog2(H);
     wp.cs = cs;
+    wp.inv_cs = 1.0f / cs;
     if (s.world_box) {
       wp.has_box = 1;
       wp.box_lo_x = s.world_box[4 * w + 0];
@@ -439,7 +456,18 @@ template <class T> cudaError_t up(T* dst, const std::vector<T>& src, cudaStream_
 
 // Lay out (or size) every device array of the scene.
 void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t nb, uint32_t nc, uint32_t ns,
-           uint32_t nj, uint32_t nw, uint32_t ncirc, uint32_t n_cells, uint32_t n_tiles) {
+           uint32_t nj, uint32_t nw, uint32_t ncirc, uint32_t n_cells, uint32_t n_tiles, bool sorted_storage) {
+  const uint32_t ss = sorted_storage ? nb : 0u;
+  d.sa[0] = cv.take<float4>(ss);
+  d.sa[1] = cv.take<float4>(ss);
+  d.sb[0] = cv.take<float4>(ss);
+  d.sb[1] = cv.take<float4>(ss);
+  d.sv[0] = cv.take<float2>(ss);
+  d.sv[1] = cv.take<float2>(ss);
+  d.body_c = cv.take<float4>(ss);
+  d.key = cv.take<uint32_t>(ss);
+  d.ckey = cv.take<uint32_t>(ss);
+  d.where = cv.take<uint32_t>(ss);
   pos[0] = cv.take<float2>(nb);
   pos[1] = cv.take<float2>(nb);
   d.pos_old = cv.take<float2>(nb);
@@ -484,8 +512,8 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t 
   d.cell_count = cv.take<uint32_t>(n_cells);
   d.cell_start = cv.take<uint32_t>((size_t)n_cells + 1);
   d.rank = cv.take<uint32_t>(nc);
-  d.sorted = cv.take<float4>(nc);
-  d.tile_state = cv.take<unsigned long long>(n_tiles);
+  d.sorted = cv.take<float4>(sorted_storage ? 0u : nc);
+  d.tile_sums = cv.take<uint32_t>(n_tiles);
   *counters = cv.take<Counters>(1);
 }
 
@@ -529,6 +557,38 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
     mark_end(w);
     w->enqueued += (uint64_t)w->cfg.joint_iterations * n_colours;
   };
+  if (w->sorted_storage) {
+    const int cur = (int)w->cur;
+    if (coll) {
+      if (!w->keys_valid) {
+        launch_keys_single(d, cur, w->multiworld, st);
+        w->enqueued += 1;
+      }
+      mark_begin(w, PHASE_SCAN);
+      launch_scan(d, st);
+      mark_end(w);
+      mark_begin(w, PHASE_SCATTER);
+      launch_permute(d, cur, w->has_springs, st);
+      mark_end(w);
+      mark_begin(w, PHASE_CONTACT);
+      launch_step_single(d, cur ^ 1, cur, w->multiworld, w->has_springs, pending, true, dt, old_dt, true,
+                         w->rot_dynamic, st);
+      mark_end(w);
+      w->enqueued += 4;  // two scan kernels, permute, step
+      w->keys_valid = true;
+      w->v_div = w->has_springs ? 0.0f : dt;
+    } else {
+      mark_begin(w, PHASE_INTEGRATE);
+      launch_step_single(d, cur, cur ^ 1, w->multiworld, w->has_springs, pending, false, dt, old_dt, false,
+                         w->rot_dynamic, st);
+      mark_end(w);
+      w->enqueued += 1;
+      w->keys_valid = false;
+      w->v_div = w->has_springs ? 0.0f : dt;
+      w->cur ^= 1u;
+    }
+    return;
+  }
   if (coll && !w->keys_valid) {
     launch_keys(d, w->multiworld, st);
     w->enqueued += 1;
@@ -537,7 +597,7 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
     mark_begin(w, PHASE_SCAN);
     launch_scan(d, st);
     mark_end(w);
-    w->enqueued += 1;
+    w->enqueued += 2;
   }
   if (coll || w->has_springs) {
     mark_begin(w, PHASE_SCATTER);
@@ -596,7 +656,8 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
   const float step_delta = delta / (float)w->cfg.substeps;
   const bool coll = w->cfg.collisions_enabled && w->nc > 0;
   if (coll && !w->keys_valid) {
-    launch_keys(w->dev, w->multiworld, w->st());
+    if (w->sorted_storage) launch_keys_single(w->dev, (int)w->cur, w->multiworld, w->st());
+    else launch_keys(w->dev, w->multiworld, w->st());
     w->keys_valid = true;
   }
   GraphKey key{f2bits(delta), w->cur, n_steps, w->timing ? 1u : 0u};
@@ -632,7 +693,10 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
     if (std::find(w->launched_sets.begin(), w->launched_sets.end(), ts) == w->launched_sets.end())
       w->launched_sets.push_back(ts);
   }
-  w->cur = cur0 ^ ((n_steps * w->cfg.substeps) & 1u);
+  // the sorted-storage path returns to its buffer every substep with contacts
+  const bool flips = !(w->sorted_storage && coll);
+  w->cur = flips ? (cur0 ^ ((n_steps * w->cfg.substeps) & 1u)) : cur0;
+  if (w->sorted_storage) w->v_div = w->has_springs ? 0.0f : step_delta;
   w->keys_valid = coll;
   return BLOBS_OK;
 }
@@ -789,12 +853,13 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   WorldDev d{};
   Counters* counters = nullptr;
   Carver sizer;
-  carve(sizer, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles);
+  const bool sorted_storage = h.single && nj == 0;
+  carve(sizer, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   e = cudaMalloc(&w->arena, sizer.off + 256);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   Carver cv;
   cv.base = static_cast<char*>(w->arena);
-  carve(cv, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles);
+  carve(cv, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   d.n_bodies = nb;
   d.n_cols = nc;
   d.n_springs = ns;
@@ -804,11 +869,10 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   d.n_cells = h.n_cells;
   d.n_tiles = n_tiles;
   d.gravity = v2(w->cfg.gravity[0], w->cfg.gravity[1]);
-  d.contacts_total = &counters->contacts_total;
-  d.pushouts_total = &counters->pushouts_total;
-  d.contacts_sub = &counters->contacts_sub;
+  d.contacts_total = counters->contacts_total;
+  d.pushouts_total = counters->pushouts_total;
+  d.contacts_sub = counters->contacts_sub;
   d.status = &counters->status;
-  d.tile_counter = &counters->tile_counter;
   w->dcounters = counters;
 
   cudaStream_t s = w->stream;
@@ -855,8 +919,34 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   UP(d.circles, h.circles);
   UP(d.wparam, h.wparam);
 #undef UP
+  std::vector<float4> sa, sb, sc;
+  std::vector<uint32_t> ident;
+  if (sorted_storage) {
+    // storage order = arena order until the first substep sorts it
+    sa.resize(nb);
+    sb.resize(nb);
+    sc.resize(nb);
+    ident.resize(nb);
+    for (uint32_t i = 0; i < nb; ++i) {
+      uint32_t idbits = i;
+      float idf;
+      std::memcpy(&idf, &idbits, 4);
+      sa[i] = make_float4(h.snap[i].x, h.snap[i].y, h.col_radius[i], idf);
+      sb[i] = make_float4(h.pos[i].x, h.pos[i].y, h.pos_old[i].x, h.pos_old[i].y);
+      const uint32_t fw = (uint32_t)h.bflags[i] | (h.body_world[i] << 8);
+      float fwf;
+      std::memcpy(&fwf, &fw, 4);
+      sc[i] = make_float4(h.mass[i], h.gmod[i], h.bound_r[i], fwf);
+      ident[i] = i;
+    }
+    if (nw >= (1u << 24)) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess) e = up(d.sa[0], sa, s);
+    if (e == cudaSuccess) e = up(d.sb[0], sb, s);
+    if (e == cudaSuccess) e = up(d.sv[0], h.vel, s);
+    if (e == cudaSuccess) e = up(d.body_c, sc, s);
+    if (e == cudaSuccess) e = up(d.where, ident, s);
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)h.n_cells, s);
-  if (e == cudaSuccess && n_tiles) e = cudaMemsetAsync(d.tile_state, 0, sizeof(unsigned long long) * n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(Counters), s);
   if (e != cudaSuccess) {
     cudaFree(w->arena);
@@ -872,6 +962,8 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   w->ncirc = ncirc;
   w->multiworld = nw > 1;
   w->single = h.single;
+  w->sorted_storage = sorted_storage;
+  w->v_div = 0.0f;
   w->has_springs = ns > 0;
   w->has_joints = nj > 0;
   w->rot_dynamic = h.rot_dynamic;
@@ -931,7 +1023,15 @@ int blobs_world_read_bodies(blobs_world* w, float* pos, float* pos_old, float* v
   const size_t n = w->nb;
   cudaError_t e = cudaSuccess;
   cudaStream_t s = w->st();
-  if (pos && n) e = cudaMemcpyAsync(pos, w->pos[w->cur], n * 8, cudaMemcpyDeviceToHost, s);
+  if (w->sorted_storage) {
+    // storage order -> arena order into the staging arrays, then copy out
+    launch_gather_single(w->dev, (int)w->cur, pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr,
+                         vel ? w->dev.vel : nullptr, nullptr, w->v_div, s);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && pos && n) e = cudaMemcpyAsync(pos, w->pos[0], n * 8, cudaMemcpyDeviceToHost, s);
+  } else if (pos && n) {
+    e = cudaMemcpyAsync(pos, w->pos[w->cur], n * 8, cudaMemcpyDeviceToHost, s);
+  }
   if (e == cudaSuccess && pos_old && n) e = cudaMemcpyAsync(pos_old, w->dev.pos_old, n * 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && vel && n) e = cudaMemcpyAsync(vel, w->dev.vel, n * 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && rotation && n) e = cudaMemcpyAsync(rotation, w->dev.rot, n * 4, cudaMemcpyDeviceToHost, s);
@@ -946,7 +1046,11 @@ int blobs_world_read_snapshots(blobs_world* w, float* xy) {
   if (!xy) return BLOBS_ERR_INVALID_ARGUMENT;
   cudaSetDevice(w->cfg.device);
   cudaError_t e = cudaSuccess;
-  if (w->nc) e = cudaMemcpyAsync(xy, w->dev.snap, (size_t)w->nc * 8, cudaMemcpyDeviceToHost, w->st());
+  if (w->sorted_storage) {
+    launch_gather_single(w->dev, (int)w->cur, nullptr, nullptr, nullptr, w->dev.snap, 0.0f, w->st());
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && w->nc) e = cudaMemcpyAsync(xy, w->dev.snap, (size_t)w->nc * 8, cudaMemcpyDeviceToHost, w->st());
   if (e != cudaSuccess) return blobs_map_cuda(e);
   return read_status(w);
 }
@@ -956,8 +1060,8 @@ int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_su
   if (!w->loaded) return BLOBS_ERR_STATE;
   cudaSetDevice(w->cfg.device);
   int st = read_status(w);
-  if (total) *total = w->hcounters->contacts_total;
-  if (last_substep) *last_substep = w->hcounters->contacts_sub;
+  if (total) *total = w->hcounters->contacts();
+  if (last_substep) *last_substep = w->hcounters->sub();
   return st;
 }
 
@@ -966,7 +1070,7 @@ int blobs_world_pushout_count(blobs_world* w, uint64_t* total) {
   if (!w->loaded) return BLOBS_ERR_STATE;
   cudaSetDevice(w->cfg.device);
   int st = read_status(w);
-  if (total) *total = w->hcounters->pushouts_total;
+  if (total) *total = w->hcounters->pushouts();
   return st;
 }
 
@@ -1004,9 +1108,17 @@ int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_
   const size_t n = w->nb;
   cudaStream_t s = w->st();
   cudaError_t e = cudaSuccess;
-  if (pos && n) e = cudaMemcpyAsync(w->pos[w->cur], pos, n * 8, cudaMemcpyHostToDevice, s);
+  float2* pos_dst = w->sorted_storage ? w->pos[0] : w->pos[w->cur];
+  if (pos && n) e = cudaMemcpyAsync(pos_dst, pos, n * 8, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && pos_old && n) e = cudaMemcpyAsync(w->dev.pos_old, pos_old, n * 8, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && vel && n) e = cudaMemcpyAsync(w->dev.vel, vel, n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && w->sorted_storage && n) {
+    // arena order staging -> storage order
+    launch_write_single(w->dev, (int)w->cur, pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr,
+                        vel ? w->dev.vel : nullptr, s);
+    if (vel) w->v_div = 0.0f;  // every V entry is now a velocity
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess && rotation && n) e = cudaMemcpyAsync(w->dev.rot, rotation, n * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && angvel && n) {
     e = cudaMemcpyAsync(w->dev.angvel, angvel, n * 4, cudaMemcpyHostToDevice, s);
@@ -1016,6 +1128,69 @@ int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_
     }
   }
   return blobs_map_cuda(e);
+}
+
+int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, uint64_t cap, uint64_t* n_pairs) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (!n_pairs || (cap && !pairs)) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  cudaStream_t s = w->st();
+  *n_pairs = 0;
+  if (w->nc == 0) return read_status(w);
+  // rebuild the cell ranges from the current snapshots; the next substep
+  // recomputes its ranks (the scan consumed the counts)
+  WorldDev dv = w->dev;
+  if (w->sorted_storage) {
+    if (!w->keys_valid) launch_keys_single(w->dev, (int)w->cur, w->multiworld, s);
+    launch_scan(w->dev, s);
+    launch_permute(w->dev, (int)w->cur, w->has_springs, s);
+    w->cur ^= 1u;  // the permuted storage becomes current
+    dv.sorted = w->dev.sa[w->cur];
+  } else {
+    if (!w->keys_valid) launch_keys(w->dev, w->multiworld, s);
+    launch_scan(w->dev, s);
+    launch_scatter_forces(w->dev, w->pos[w->cur], w->multiworld, true, false, false, s);
+  }
+  w->keys_valid = false;
+  uint32_t* dpairs = nullptr;
+  unsigned long long* dcount = nullptr;
+  cudaError_t e = cudaMallocAsync(&dcount, sizeof(unsigned long long), s);
+  if (e == cudaSuccess && cap) e = cudaMallocAsync(&dpairs, 2 * sizeof(uint32_t) * cap, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) {
+    launch_emit_pairs(dv, w->multiworld, contacts_only ? 1u : 0u, dpairs, cap, dcount, s);
+    e = cudaGetLastError();
+  }
+  unsigned long long total = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, dcount, sizeof(total), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && cap)
+    e = cudaMemcpyAsync(pairs, dpairs, 2 * sizeof(uint32_t) * (total < cap ? total : cap), cudaMemcpyDeviceToHost, s);
+  if (dpairs) cudaFreeAsync(dpairs, s);
+  if (dcount) cudaFreeAsync(dcount, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  *n_pairs = total;
+  int st = read_status(w);
+  if (st) return st;
+  return total > cap ? BLOBS_ERR_OVERFLOW : BLOBS_OK;
+}
+
+int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, uint32_t* log2_width,
+                     uint32_t* log2_height) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (world >= w->nw) return BLOBS_ERR_INVALID_ARGUMENT;
+  WorldParam wp;
+  cudaSetDevice(w->cfg.device);
+  cudaError_t e = cudaMemcpy(&wp, w->dev.wparam + world, sizeof(wp), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  if (cell_size) *cell_size = wp.cs;
+  if (inv_cell_size) *inv_cell_size = wp.inv_cs;
+  if (log2_width) *log2_width = wp.log2w;
+  if (log2_height) *log2_height = wp.log2h;
+  return BLOBS_OK;
 }
 
 int blobs_world_kernel_launches(blobs_world* w, uint64_t* count) {

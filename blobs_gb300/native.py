@@ -98,6 +98,9 @@ def lib() -> ctypes.CDLL:
         "blobs_world_set_stream": (i32, [_P, _P]),
         "blobs_world_write_bodies": (i32, [_P, _P, _P, _P, _P, _P]),
         "blobs_world_set_timing": (i32, [_P, i32]),
+        "blobs_world_emit_pairs": (i32, [_P, i32, _P, u64, ctypes.POINTER(u64)]),
+        "blobs_world_grid": (i32, [_P, u32, ctypes.POINTER(f32), ctypes.POINTER(f32), ctypes.POINTER(u32),
+                                   ctypes.POINTER(u32)]),
         "blobs_world_kernel_launches": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_phase_times": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(u64), u32]),
     }
@@ -283,6 +286,28 @@ class World:
 
     def set_timing(self, enabled: bool) -> None:
         check(lib().blobs_world_set_timing(self._h, 1 if enabled else 0), "set_timing")
+
+    def emit_pairs(self, contacts_only: bool, cap: Optional[int] = None):
+        """(hi, lo) collider pairs of the broadphase (see blobs_world_emit_pairs),
+        sorted; grows the buffer once on BLOBS_ERR_OVERFLOW."""
+        n = ctypes.c_uint64()
+        cap = 1024 if cap is None else cap
+        buf = np.zeros((max(cap, 1), 2), np.uint32)
+        st = lib().blobs_world_emit_pairs(self._h, 1 if contacts_only else 0, _ptr(buf), cap, ctypes.byref(n))
+        if st == ERR_OVERFLOW:
+            buf = np.zeros((max(int(n.value), 1), 2), np.uint32)
+            st = lib().blobs_world_emit_pairs(self._h, 1 if contacts_only else 0, _ptr(buf), int(n.value),
+                                              ctypes.byref(n))
+        check(st, "emit_pairs")
+        out = buf[:int(n.value)]
+        return out[np.lexsort((out[:, 1], out[:, 0]))]
+
+    def grid(self, world: int = 0):
+        """(cell size, f32 reciprocal, log2 width, log2 height) of a world's grid."""
+        cs, inv, lw, lh = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().blobs_world_grid(self._h, world, ctypes.byref(cs), ctypes.byref(inv), ctypes.byref(lw),
+                                     ctypes.byref(lh)), "grid")
+        return cs.value, inv.value, lw.value, lh.value
 
     def kernel_launches(self) -> int:
         n = ctypes.c_uint64()

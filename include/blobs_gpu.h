@@ -210,6 +210,19 @@ int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_su
 /* Contacts resolved with the coincident-centre push-out branch
  * (physics.rs:272-286) since load. */
 int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
+/* The broadphase output for the current collider snapshots: every collider
+ * pair (hi, lo), hi > lo in arena order, whose cells are 3x3 neighbours in
+ * its world's grid (contacts_only = 0), or only the pairs the contact pass
+ * resolves (contacts_only = 1: different parents, InteractionGroups::test,
+ * distance < ra + rb -- the pair set of brute_force_collisions,
+ * physics.rs:248-269).  Unordered; `pairs` holds 2 * cap entries.  Returns
+ * BLOBS_ERR_OVERFLOW with *n_pairs = the full count when cap is too small. */
+int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, uint64_t cap, uint64_t* n_pairs);
+/* The toroidal cell grid of world `world`: cell edge, its f32 reciprocal,
+ * and log2 of the width and height in cells (cell (ix, iy) =
+ * floor(v * inv_cell_size) wrapped mod 2^log2). */
+int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, uint32_t* log2_width,
+                     uint32_t* log2_height);
 /* Physics.time and the accumulator of fixed_step. */
 int blobs_world_time(blobs_world* w, double* time, double* accumulator);
 /* The joint processing order the GPU schedule uses (graph colouring: joints
