@@ -36,6 +36,9 @@ struct WorldParam {
   float box_lo_x, box_lo_y, box_hi_x, box_hi_y;
   uint32_t has_box;     // axis-aligned wall extension enabled
   float inv_cs;         // 1 / cs (rounded once, on the host)
+  uint32_t first_dyn;   // arena id of the world's first non-static body (uniform single-sphere worlds)
+  float uniform_gmod;   // gravity_mod shared by every body (uniform single-sphere worlds)
+  float ox, oy;         // grid origin: the world's extent maps to cells 1 .. W-2, away from the wrap
   uint32_t pad[2];
 };
 
@@ -99,10 +102,11 @@ struct WorldDev {
   float4* sorted;            // per slot: (x, y, radius, collider index bits)
   uint32_t* tile_sums;       // per scan tile
 
-  // single-sphere path: cell-sorted body storage, double-buffered
-  float4* sa[2];             // (snapshot x, y, radius, arena id bits)
+  // single-sphere path: body storage re-sorted into cell order once per step
+  float4* sa[2];             // (snapshot x, y, radius, arena id bits), double-buffered per substep
   float4* sb[2];             // (position x, y, position_old x, y)
-  float2* sv[2];             // calculated_velocity
+  float2* sv[2];             // calculated_velocity (or the last substep's displacement)
+  float4* cand;              // cell-order copy of sa: the candidate records of a substep
   float4* body_c;            // arena order: (mass, gravity_mod, bounding radius, flags | world << 8)
   uint32_t* key;             // per storage slot: cell of the snapshot for the next substep
   uint32_t* ckey;            // per storage slot: cell the permute sorted the body into
@@ -148,10 +152,11 @@ __device__ __host__ __forceinline__ int32_t grid_coord(float v, float inv_cs) {
   return (int32_t)q;
 }
 
-// Global cell index of a point in world `wp`'s toroidal grid.
+// Global cell index of a point in world `wp`'s toroidal grid:
+// cell = floor((v - origin) * (1/cs)) wrapped mod the grid size.
 __device__ __host__ __forceinline__ uint32_t cell_key(const WorldParam& wp, float2 s) {
-  uint32_t ix = (uint32_t)grid_coord(s.x, wp.inv_cs) & ((1u << wp.log2w) - 1u);
-  uint32_t iy = (uint32_t)grid_coord(s.y, wp.inv_cs) & ((1u << wp.log2h) - 1u);
+  uint32_t ix = (uint32_t)grid_coord(s.x - wp.ox, wp.inv_cs) & ((1u << wp.log2w) - 1u);
+  uint32_t iy = (uint32_t)grid_coord(s.y - wp.oy, wp.inv_cs) & ((1u << wp.log2h) - 1u);
   return wp.cell_base + ((iy << wp.log2w) | ix);
 }
 
@@ -172,6 +177,20 @@ struct SubstepArgs {
   float ratio_rest;      // dt / dt (exactly 1 for a finite non-zero dt)
   uint32_t do_keys;
   uint32_t rot_dynamic;  // 0: every angular velocity is 0 and no torque is pending -> rotation is constant
+};
+
+// Launch arguments of the single-sphere kernels.
+struct SingleArgs {
+  const float4* a_in;
+  const float4* b_in;
+  const float2* v_in;
+  float4* a_out;
+  float4* b_out;
+  float2* v_out;
+  const float4* cand;        // candidate records in cell order
+  const uint32_t* own_cell;  // cell of each storage slot in this substep's order
+  float dt, ratio_first, ratio_rest;
+  uint32_t contacts, pending, springs, rot_dynamic, do_keys, write_v, move_v;
 };
 
 constexpr int SCAN_THREADS = 256;

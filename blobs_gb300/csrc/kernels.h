@@ -20,15 +20,15 @@ void launch_integrate(const WorldDev& w, const float2* pos_in, float2* pos_out, 
 void launch_emit_pairs(const WorldDev& w, bool multiworld, uint32_t mode, uint32_t* out, unsigned long long cap,
                        unsigned long long* count, cudaStream_t st);
 
-// single-sphere path with cell-sorted storage (single.cu)
-void launch_permute(const WorldDev& w, int from, bool springs, cudaStream_t st);
-void launch_step_single(const WorldDev& w, int from, int to, bool multiworld, bool springs, bool pending,
-                        bool contacts, float dt, float old_dt, bool do_keys, bool rot_dynamic, cudaStream_t st);
-void launch_keys_single(const WorldDev& w, int cur, bool multiworld, cudaStream_t st);
-void launch_gather_single(const WorldDev& w, int cur, float2* pos, float2* pos_old, float2* vel, float2* snap,
-                          float v_div, cudaStream_t st);
-void launch_write_single(const WorldDev& w, int cur, const float2* pos, const float2* pos_old, const float2* vel,
-                         cudaStream_t st);
-void launch_where_single(const WorldDev& w, int cur, cudaStream_t st);
+// single-sphere path with cell-sorted storage (single.cu); mode 0: one
+// uniform world, 1: one world with per-body records, 2: batched worlds
+void launch_permute(const WorldDev& w, const SingleArgs& a, cudaStream_t st);
+void launch_scatter_cand(const WorldDev& w, const float4* a_in, float4* cand, cudaStream_t st);
+void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st);
+void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st);
+void launch_gather_single(const WorldDev& w, const float4* A, const float4* B, const float2* V, float2* pos,
+                          float2* pos_old, float2* vel, float2* snap, float v_div, cudaStream_t st);
+void launch_write_single(const WorldDev& w, const float4* A, float4* B, float2* V, const float2* pos,
+                         const float2* pos_old, const float2* vel, cudaStream_t st);
 
 }  // namespace blobs

@@ -1,6 +1,6 @@
 // physics.cpp -- the C++ host mirror of the reference Physics API
 // (include/blobs_physics.hpp) on top of the C ABI (include/blobs_gpu.h).
-#include "../../include/blobs_physics.hpp"
+#include "blobs_physics.hpp"
 
 #include <cstring>
 

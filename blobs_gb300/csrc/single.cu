@@ -1,21 +1,21 @@
 // single.cu -- the single-sphere path: every body owns exactly one collider
 // at offset zero with default groups and no sensor, and there are no fixed
-// joints (configurations 1, 2, 4 and 5).  Body state lives in cell-sorted
-// storage order, so the contact gather and the integration read and write
-// it coalesced:
+// joints (configurations 1, 2, 4 and 5).
 //
-//   k_permute      storage slot i of the previous substep -> slot
-//                  cell_start[key] + rank of this substep (counting-sort
-//                  scatter of the whole body record; bodies move little per
-//                  substep, so the writes are nearly coalesced)
+// Body state lives in "storage order", re-sorted into cell order once per
+// step, so that a warp's bodies are spatial neighbours:
+//   A[slot] = (snapshot x, snapshot y, radius, arena id bits)
+//   B[slot] = (position x, y, position_old x, y)
+//   V[slot] = calculated_velocity (or, without springs, the last
+//             substep's displacement; the division by dt happens on read)
+// A, B, V are double-buffered per substep.  Per substep:
+//   k_permute      (first substep of a step) storage -> this substep's cell
+//                  order; the permuted A is then also the candidate array
+//   k_scatter_cand (other substeps) a cell-order copy of A for the
+//                  candidate search (16 B per body instead of the record)
 //   k_step_single  per slot: gravity + springs, contacts over the 3x3 cells
 //                  applied in the reference's pair order, Verlet
-//                  integration, constraints, and the cell key / rank of the
-//                  next substep
-//
-// Records: A = (snapshot x, snapshot y, radius, arena id bits),
-//          B = (position x, y, position_old x, y), V = calculated_velocity,
-//          body_c[id] = (mass, gravity_mod, bounding radius, flags | world << 8).
+//                  integration, constraints, next cell key / rank
 // Compiled with --fmad=false (see device.cuh).
 #include "device.cuh"
 #include "kernels.h"
@@ -27,8 +27,8 @@ namespace {
 __device__ __forceinline__ uint32_t rec_flags(float4 c) { return __float_as_uint(c.w) & 0xffu; }
 __device__ __forceinline__ uint32_t rec_world(float4 c) { return __float_as_uint(c.w) >> 8; }
 
-// The cell-sorted slots of the 3 rows of 3 cells around point s: up to six
-// contiguous segments (a row splits in two where the torus wraps).
+// The cell-order positions of the 3 rows of 3 cells around cell `key`: up to
+// six contiguous segments (a row splits in two where the torus wraps).
 struct Segments {
   uint32_t s[6], l[6];
 };
@@ -64,7 +64,7 @@ __device__ __forceinline__ Segments segments(const WorldDev& w, const WorldParam
   return g;
 }
 
-// Slot of the t-th candidate of the segments (t < total).
+// Position of the t-th candidate of the segments (t < total).
 __device__ __forceinline__ uint32_t slot_of(const Segments& g, uint32_t t) {
   uint32_t q = g.s[5] + t;
   uint32_t acc = 0;
@@ -78,34 +78,32 @@ __device__ __forceinline__ uint32_t slot_of(const Segments& g, uint32_t t) {
   return q;
 }
 
-// Visit every slot of the segments in one flattened loop (less divergence
-// than a loop per row).
-template <class F>
-__device__ __forceinline__ void visit(const Segments& g, F&& f) {
-  const uint32_t total = g.l[0] + g.l[1] + g.l[2] + g.l[3] + g.l[4] + g.l[5];
-  uint32_t seg = 0, q = g.s[0], left = g.l[0];
-  for (uint32_t t = 0; t < total; ++t) {
-    while (left == 0u) {
-      ++seg;
-      switch (seg) {
-        case 1: q = g.s[1]; left = g.l[1]; break;
-        case 2: q = g.s[2]; left = g.l[2]; break;
-        case 3: q = g.s[3]; left = g.l[3]; break;
-        case 4: q = g.s[4]; left = g.l[4]; break;
-        default: q = g.s[5]; left = g.l[5]; break;
-      }
-    }
-    f(q);
-    ++q;
-    --left;
+// Near test of four consecutive candidate positions [q, q + 4) clipped to
+// `en`, loads issued together for memory-level parallelism.
+__device__ __forceinline__ bool near_pair(float dx, float dy, float mind);
+
+__device__ __forceinline__ void near_range(const float4* __restrict__ C, float2 s, float r, uint32_t st, uint32_t en,
+                                           uint32_t& t, unsigned long long& near) {
+  for (uint32_t q = st; q < en; q += 4u, t += 4u) {
+    const float4 far = make_float4(3.0e38f, 3.0e38f, 0.0f, 0.0f);
+    const float4 o0 = C[q];
+    const float4 o1 = q + 1u < en ? C[q + 1u] : far;
+    const float4 o2 = q + 2u < en ? C[q + 2u] : far;
+    const float4 o3 = q + 3u < en ? C[q + 3u] : far;
+    unsigned long long m = 0ull;
+    if (near_pair(s.x - o0.x, s.y - o0.y, r + o0.z)) m |= 1ull;
+    if (near_pair(s.x - o1.x, s.y - o1.y, r + o1.z)) m |= 2ull;
+    if (near_pair(s.x - o2.x, s.y - o2.y, r + o2.z)) m |= 4ull;
+    if (near_pair(s.x - o3.x, s.y - o3.y, r + o3.z)) m |= 8ull;
+    near |= m << t;
   }
 }
 
 // Exact contact test of the reference (physics.rs:264-269): sqrt(d.d) < ra + rb.
 // A squared-distance test rejects first: T >= (ra + rb)^2 strictly, so
 // d.d > T implies sqrt(d.d) >= ra + rb and the reference rejects too.
-__device__ __forceinline__ bool near_pair(float dx, float dy, float mind, float& D) {
-  D = (dx * dx) + (dy * dy);
+__device__ __forceinline__ bool near_pair(float dx, float dy, float mind) {
+  const float D = (dx * dx) + (dy * dy);
   const float T = (mind * mind) * 1.00000024f;
   return !(D > T);
 }
@@ -116,25 +114,24 @@ struct SinglePair {
   bool pushed;
 };
 
-// One contact of body `c` (at p, snapshot s, radius r, mass m) with body c2
-// (snapshot s2, radius r2): the increment to c's position.  Returns false if
-// not in contact.  Push-out (physics.rs:272-286) uses positions at the start
-// of the contact pass.
-__device__ __forceinline__ bool single_pair(const WorldDev& w, uint32_t c, float2 p, float2 s, float r, float m,
-                                            uint32_t c2, const float4* __restrict__ B, uint32_t q, float2 s2,
-                                            float r2, SinglePair& out) {
+// The increment to body c's position from its contact with body c2, in the
+// reference's terms (a = the higher arena index).  Returns false if the pair
+// is not in contact.  The push-out branch (physics.rs:272-286) uses the
+// positions at the start of the contact pass.
+__device__ __forceinline__ bool single_pair(const WorldDev& w, const SingleArgs& a, uint32_t c, float2 p, float2 s,
+                                            float r, float m, uint32_t c2, float2 s2, float r2, float m2,
+                                            SinglePair& out) {
   const float dx = s.x - s2.x, dy = s.y - s2.y;
-  float D;
   const float mind = r + r2;
-  if (!near_pair(dx, dy, mind, D)) return false;
-  float d = sqrtf(D);
+  float d = sqrtf((dx * dx) + (dy * dy));
   if (!(d < mind)) return false;
   const bool hi = c > c2;
   float2 axis = hi ? v2(dx, dy) : v2(-dx, -dy);
   out.pushed = false;
   out.push = v2(0.0f, 0.0f);
   if (d < 1e-6f) {
-    const float2 p2 = v2(B[q].x, B[q].y);
+    const float4 b2 = a.b_in[w.where[c2]];
+    const float2 p2 = v2(b2.x, b2.y);
     const float2 pa = add(hi ? p : p2, v2(0.01f, 0.0f));
     const float2 pb = sub(hi ? p2 : p, v2(0.01f, 0.0f));
     axis = sub(add(pa, v2(0.0f, 0.0f)), add(pb, v2(0.0f, 0.0f)));
@@ -145,7 +142,6 @@ __device__ __forceinline__ bool single_pair(const WorldDev& w, uint32_t c, float
   const float2 n = divs(axis, d);
   if (n.x != n.x || n.y != n.y) atomicOr(w.status, ST_NAN);
   const float delta = mind - d;
-  const float m2 = w.body_c[c2].x;
   const float ma = hi ? m : m2, mb = hi ? m2 : m;
   const float ratio = 1.0f - ma / (ma + mb);
   if (hi) {
@@ -174,14 +170,82 @@ __device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts
   }
 }
 
+// Mass, gravity_mod, bounding radius, flags and world of the body with
+// arena id c.  A uniform world (default collider masses, no static body, one
+// gravity_mod, one world) needs no per-body record: the reference's mass of
+// a lone sphere is (0 + 2r) + 2r = 4r exactly (rigid_body.rs:96-128 with the
+// doubled handle), its bounding radius |0| + r = r.
+struct BodyConst {
+  float m, gm, br;
+  uint32_t flags, world;
+};
+
+template <int MODE>  // 0: one world, uniform; 1: one world, per-body record; 2: batched, per-body record
+__device__ __forceinline__ BodyConst body_const(const WorldDev& w, const WorldParam& wp0, uint32_t c, float r) {
+  BodyConst k;
+  if (MODE == 0) {
+    k.m = r * 4.0f;
+    k.gm = wp0.uniform_gmod;
+    k.br = r;
+    k.flags = (c == wp0.first_dyn) ? (uint32_t)BF_FIRST_DYN : 0u;
+    k.world = 0u;
+  } else {
+    const float4 rec = w.body_c[c];
+    k.m = rec.x;
+    k.gm = rec.y;
+    k.br = rec.z;
+    k.flags = rec_flags(rec);
+    k.world = MODE == 2 ? rec_world(rec) : 0u;
+  }
+  return k;
+}
+
+// Exact selection walk over all candidates of the segments, in ascending
+// arena id (many candidates, or any layout): O(contacts x candidates).
+template <int MODE>
+__device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Segments& g, uint32_t j, uint32_t c,
+                                float2 p0, float2 s, float r, float m, uint32_t& ncontacts, uint32_t& npush) {
+  const float4* __restrict__ C = a.cand;
+  float2 p = p0;
+  uint32_t last = 0u;
+  bool first = true;
+  while (true) {
+    uint32_t best = 0xffffffffu;
+    float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool found = false;
+    for (int sg = 0; sg < 6; ++sg) {
+      const uint32_t q1 = g.s[sg] + g.l[sg];
+      for (uint32_t q = g.s[sg]; q < q1; ++q) {
+        const float4 o = C[q];
+        const uint32_t c2 = __float_as_uint(o.w);
+        if (c2 == c || c2 >= w.n_bodies || (!first && c2 <= last) || (found && c2 >= best)) continue;
+        const float dx = s.x - o.x, dy = s.y - o.y;
+        if (!(sqrtf((dx * dx) + (dy * dy)) < r + o.z)) continue;
+        best = c2;
+        bo = o;
+        found = true;
+      }
+    }
+    if (!found) break;
+    const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
+    SinglePair sp;
+    single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp);
+    if (sp.pushed) p = add(p, sp.push);
+    p = add(p, sp.corr);
+    if (best < c) {
+      ++ncontacts;
+      npush += sp.pushed ? 1u : 0u;
+    }
+    last = best;
+    first = false;
+  }
+  return p;
+}
 
 }  // namespace
 
-template <bool SPR>
-__global__ void __launch_bounds__(256) k_permute(WorldDev w, const float4* __restrict__ a_in,
-                                                 const float4* __restrict__ b_in, const float2* __restrict__ v_in,
-                                                 float4* __restrict__ a_out, float4* __restrict__ b_out,
-                                                 float2* __restrict__ v_out) {
+// Storage slot i -> its position in this substep's cell order.
+__global__ void __launch_bounds__(256) k_permute(WorldDev w, SingleArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= w.n_bodies) return;
   const uint32_t key = w.key[i];
@@ -190,81 +254,96 @@ __global__ void __launch_bounds__(256) k_permute(WorldDev w, const float4* __res
     atomicOr(w.status, ST_BAD_INDEX);
     return;
   }
-  const float4 a = a_in[i];
-  a_out[j] = a;
-  b_out[j] = b_in[i];
+  const float4 av = a.a_in[i];
+  a.a_out[j] = av;
+  a.b_out[j] = a.b_in[i];
+  if (a.move_v) a.v_out[j] = a.v_in[i];
   w.ckey[j] = key;
-  if (SPR) {
-    v_out[j] = v_in[i];
-    const uint32_t id = __float_as_uint(a.w);
-    if (id < w.n_bodies) w.where[id] = j;
-  }
+  const uint32_t id = __float_as_uint(av.w);
+  if (id < w.n_bodies) w.where[id] = j;
 }
 
-template <bool MW, bool SPR, bool PEND, bool CONTACTS>
-__global__ void __launch_bounds__(256) k_step_single(WorldDev w, const float4* __restrict__ A,
-                                                     const float4* __restrict__ B, const float2* __restrict__ V,
-                                                     float4* __restrict__ a_out, float4* __restrict__ b_out,
-                                                     float2* __restrict__ v_out, SubstepArgs args) {
+// Cell-order copy of the snapshot records (candidates of this substep).
+__global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* __restrict__ a_in,
+                                                      float4* __restrict__ cand) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n_bodies) return;
+  const uint32_t j = w.cell_start[w.key[i]] + w.rank[i];
+  if (j >= w.n_bodies) {
+    atomicOr(w.status, ST_BAD_INDEX);
+    return;
+  }
+  cand[j] = a_in[i];
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t ncontacts = 0, npush = 0;
   if (j < w.n_bodies) {
-    const float4 a = A[j];
-    const float4 b = B[j];
-    uint32_t c = __float_as_uint(a.w);
+    const float4 av = a.a_in[j];
+    const float4 bv = a.b_in[j];
+    uint32_t c = __float_as_uint(av.w);
     if (c >= w.n_bodies) {
       atomicOr(w.status, ST_BAD_INDEX);
       c = 0;
     }
-    const float4 rec = w.body_c[c];
-    const float m = rec.x;
-    const uint32_t fl = rec_flags(rec);
-    const WorldParam wp = w.wparam[MW ? rec_world(rec) : 0u];
-    const float2 s = v2(a.x, a.y);
-    const float r = a.z;
-    const float2 p0 = v2(b.x, b.y);  // position at the start of the substep
+    const float2 s = v2(av.x, av.y);
+    const float r = av.z;
+    const WorldParam wp0 = w.wparam[0];
+    const BodyConst k = body_const<MODE>(w, wp0, c, r);
+    const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
+    const float2 p0 = v2(bv.x, bv.y);  // position at the start of the substep
     float2 p = p0;
 
-    if (CONTACTS) {
-      const Segments g = segments(w, wp, w.ckey[j]);
-      const uint32_t total = g.l[0] + g.l[1] + g.l[2] + g.l[3] + g.l[4] + g.l[5];
-      if (total <= 64u) {
-        // Phase 1: one squared-distance test per candidate; near candidates
-        // become bits of their position in the 3x3 enumeration.
+    const uint32_t own_key = a.contacts ? a.own_cell[j] : 0u;
+    const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
+    const uint32_t lx = (own_key - wp.cell_base) & wm, ly = (own_key - wp.cell_base) >> wp.log2w;
+    const bool interior = lx >= 1u && lx < wm && ly >= 1u && ly < hm;
+    if (a.contacts && interior) {
+      // Cells away from the grid edge: the 3x3 block is three contiguous
+      // ranges of the cell-order array, one per row.
+      const float4* __restrict__ C = a.cand;
+      const uint32_t n = w.n_bodies;
+      const uint32_t r1 = own_key - 1u, r0 = r1 - (wm + 1u), r2 = r1 + (wm + 1u);
+      const uint32_t s0 = w.cell_start[r0], s1 = w.cell_start[r1], s2 = w.cell_start[r2];
+      const uint32_t e0 = min(w.cell_start[r0 + 3u], n), e1 = min(w.cell_start[r1 + 3u], n),
+                     e2 = min(w.cell_start[r2 + 3u], n);
+      const uint32_t l0 = e0 > s0 ? e0 - s0 : 0u, l1 = e1 > s1 ? e1 - s1 : 0u, l2 = e2 > s2 ? e2 - s2 : 0u;
+      // bit positions are padded to multiples of 4 per row: they must fit 64
+      if (((l0 + 3u) & ~3u) + ((l1 + 3u) & ~3u) + ((l2 + 3u) & ~3u) <= 64u) {
+        // Phase 1: squared-distance test per candidate (self included, it is
+        // skipped below); near candidates become bits of their position
+        // (row 0 at bit 0, row 1 at bit 4*ceil(l0/4), ...).
         unsigned long long near = 0ull;
         uint32_t t = 0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          const uint32_t q1 = g.s[k] + g.l[k];
-          for (uint32_t q = g.s[k]; q < q1; ++q, ++t) {
-            const float4 o = A[q];
-            const float dx = s.x - o.x, dy = s.y - o.y;
-            float D;
-            if (near_pair(dx, dy, r + o.z, D) && q != j) near |= 1ull << t;
-          }
-        }
-        // Phase 2: apply the near candidates in ascending neighbour id (the
-        // reference's pair order for this body), smallest id first.
+        near_range(C, s, r, s0, s0 + l0, t, near);
+        const uint32_t t1 = t;
+        near_range(C, s, r, s1, s1 + l1, t, near);
+        const uint32_t t2 = t;
+        near_range(C, s, r, s2, s2 + l2, t, near);
+        // Phase 2: the near candidates in ascending arena id (the
+        // reference's pair order for this body), the warp's lanes in step.
         while (near) {
           unsigned long long best_bit = 0ull;
-          uint32_t best = 0xffffffffu, bq = 0u;
+          uint32_t best = 0xffffffffu;
           float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
           for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
             const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
-            const uint32_t q = slot_of(g, tt);
-            const float4 o = A[q];
+            const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
+            const float4 o = C[q];
             const uint32_t c2 = __float_as_uint(o.w);
             if (c2 < best) {
               best = c2;
-              bq = q;
               bo = o;
               best_bit = mk & (~mk + 1ull);
             }
           }
           near &= ~best_bit;
-          if (best >= w.n_bodies) continue;
+          if (best >= w.n_bodies || best == c) continue;
+          const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
           SinglePair sp;
-          if (!single_pair(w, c, p0, s, r, m, best, B, bq, v2(bo.x, bo.y), bo.z, sp)) continue;
+          if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
           p = add(p, sp.corr);
           if (best < c) {
@@ -273,61 +352,86 @@ __global__ void __launch_bounds__(256) k_step_single(WorldDev w, const float4* _
           }
         }
       } else {
-        // more than 64 candidates: exact selection walk over all of them
-        uint32_t last = 0u;
-        bool first = true;
-        while (true) {
+        p = contacts_walk<MODE>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush);
+      }
+    } else if (a.contacts) {
+      // cells on the grid edge (the torus wraps): general segments
+      const float4* __restrict__ C = a.cand;
+      const Segments g = segments(w, wp, own_key);
+      const uint32_t total = g.l[0] + g.l[1] + g.l[2] + g.l[3] + g.l[4] + g.l[5];
+      if (total <= 64u) {
+        // Phase 1: one squared-distance test per candidate (self included:
+        // it is skipped below); near candidates become bits of their
+        // position in the 3x3 enumeration.
+        unsigned long long near = 0ull;
+        uint32_t t = 0;
+#pragma unroll
+        for (int sg = 0; sg < 6; ++sg) {
+          const uint32_t q1 = g.s[sg] + g.l[sg];
+          for (uint32_t q = g.s[sg]; q < q1; ++q, ++t) {
+            const float4 o = C[q];
+            if (near_pair(s.x - o.x, s.y - o.y, r + o.z)) near |= 1ull << t;
+          }
+        }
+        // Phase 2: the near candidates in ascending arena id (the
+        // reference's pair order for this body), the warp's lanes in step.
+        while (near) {
+          unsigned long long best_bit = 0ull;
           uint32_t best = 0xffffffffu;
-          SinglePair bo;
-          bool found = false;
-          visit(g, [&](uint32_t q) {
-            if (q == j) return;
-            const float4 o = A[q];
+          float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
+            const float4 o = C[slot_of(g, (uint32_t)(__ffsll((long long)mk) - 1))];
             const uint32_t c2 = __float_as_uint(o.w);
-            if (c2 >= w.n_bodies || (!first && c2 <= last) || (found && c2 >= best)) return;
-            SinglePair sp;
-            if (!single_pair(w, c, p0, s, r, m, c2, B, q, v2(o.x, o.y), o.z, sp)) return;
-            best = c2;
-            bo = sp;
-            found = true;
-          });
-          if (!found) break;
-          if (bo.pushed) p = add(p, bo.push);
-          p = add(p, bo.corr);
+            if (c2 < best) {
+              best = c2;
+              bo = o;
+              best_bit = mk & (~mk + 1ull);
+            }
+          }
+          near &= ~best_bit;
+          if (best >= w.n_bodies || best == c) continue;
+          const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
+          SinglePair sp;
+          if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
+          if (sp.pushed) p = add(p, sp.push);
+          p = add(p, sp.corr);
           if (best < c) {
             ++ncontacts;
-            npush += bo.pushed ? 1u : 0u;
+            npush += sp.pushed ? 1u : 0u;
           }
-          last = best;
-          first = false;
         }
+      } else {
+        p = contacts_walk<MODE>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush);
       }
     }
 
     // ---- update_objects (physics.rs:323-367) with gravity + springs ----
-    const float dt = args.dt;
+    const float dt = a.dt;
     float2 po, vel;
-    if (fl & BF_STATIC) {
+    if (k.flags & BF_STATIC) {
       po = p;
       vel = v2(0.0f, 0.0f);
     } else {
-      po = v2(b.z, b.w);
-      if (PEND && (fl & BF_VREQ)) po = sub(p, mul(w.vreq[c], dt));
-      const float ratio = (fl & BF_FIRST_DYN) ? args.ratio_first : args.ratio_rest;
+      po = v2(bv.z, bv.w);
+      uint32_t fl = k.flags;
+      if (a.pending && MODE == 0) fl |= rec_flags(w.body_c[c]);
+      if (a.pending && (fl & BF_VREQ)) po = sub(p, mul(w.vreq[c], dt));
+      const float ratio = (fl & BF_FIRST_DYN) ? a.ratio_first : a.ratio_rest;
       const float2 disp = mul(sub(p, po), ratio);
-      float2 acc = PEND ? w.pend_acc[c] : v2(0.0f, 0.0f);
-      acc = add(acc, mul(w.gravity, rec.y));
-      if (SPR) {
+      float2 acc = a.pending ? w.pend_acc[c] : v2(0.0f, 0.0f);
+      acc = add(acc, mul(w.gravity, k.gm));
+      if (a.springs) {
         const uint32_t q0 = w.body_spr_start[c], q1 = w.body_spr_start[c + 1];
         for (uint32_t qq = q0; qq < q1; ++qq) {
           const uint32_t e = w.body_spr[qq];
           const uint32_t sidx = e >> 1;
-          const uint32_t ia = w.spr_a[sidx], ib = w.spr_b[sidx];
-          const uint32_t other = (e & 1u) ? ia : ib;
+          const uint32_t other = (e & 1u) ? w.spr_a[sidx] : w.spr_b[sidx];
           const uint32_t so = w.where[other];
-          const float2 po_pos = v2(B[so].x, B[so].y);
-          const float2 po_vel = V[so];
-          const float2 va = (e & 1u) ? po_vel : V[j], vb = (e & 1u) ? V[j] : po_vel;
+          const float4 bo = a.b_in[so];
+          const float2 po_pos = v2(bo.x, bo.y);
+          const float2 po_vel = a.v_in[so];
+          const float2 own_vel = a.v_in[j];
+          const float2 va = (e & 1u) ? po_vel : own_vel, vb = (e & 1u) ? own_vel : po_vel;
           const float2 pa = (e & 1u) ? po_pos : p0, pb = (e & 1u) ? p0 : po_pos;
           const float2 d = sub(pb, pa);
           const float dist = len2(d);
@@ -338,56 +442,55 @@ __global__ void __launch_bounds__(256) k_step_single(WorldDev w, const float4* _
           const float2 fm = v2(sk - damping.x, sk - damping.y);  // springs.rs:41 broadcast
           float2 f = mulv(dir, fm);
           if (e & 1u) f = v2(-f.x, -f.y);
-          acc = add(acc, divs(f, m));
+          acc = add(acc, divs(f, k.m));
         }
       }
       po = p;
       p = add(p, add(disp, mul(mul(acc, dt), dt)));
-      if (args.rot_dynamic) {
-        const float tq = PEND ? w.pend_torque[c] : 0.0f;
-        float av = w.angvel[c];
-        av = av + (tq / w.inertia[c]) * dt;
-        w.angvel[c] = av;
-        w.rot[c] = w.rot[c] + av * dt;
+      if (a.rot_dynamic) {
+        const float tq = a.pending ? w.pend_torque[c] : 0.0f;
+        float avl = w.angvel[c];
+        avl = avl + (tq / w.inertia[c]) * dt;
+        w.angvel[c] = avl;
+        w.rot[c] = w.rot[c] + avl * dt;
       }
-      // calculated_velocity = disp / dt (physics.rs:357).  Without springs
-      // nothing reads it during the step: keep disp and divide on read.
-      vel = SPR ? divs(disp, dt) : disp;
+      // calculated_velocity = disp / dt (physics.rs:357); without springs
+      // nothing reads it during the step, so the displacement is kept and
+      // divided when it is read
+      vel = a.springs ? divs(disp, dt) : disp;
     }
     const float2 snap = v2(0.0f + p.x, 0.0f + p.y);  // rot(theta) * 0 + p
-    for (uint32_t k = 0; k < w.n_circles; ++k) {
-      const float2 cc = v2(w.circles[3 * k], w.circles[3 * k + 1]);
-      const float radius = w.circles[3 * k + 2];
+    for (uint32_t kk = 0; kk < w.n_circles; ++kk) {
+      const float2 cc = v2(w.circles[3 * kk], w.circles[3 * kk + 1]);
+      const float radius = w.circles[3 * kk + 2];
       const float2 to = sub(p, cc);
       const float dist = len2(to);
       if (dist > radius) p = add(cc, mul(divs(to, dist), radius));
     }
     if (wp.has_box) {
-      const float br = rec.z;
-      p.x = fminf(fmaxf(p.x, wp.box_lo_x + br), wp.box_hi_x - br);
-      p.y = fminf(fmaxf(p.y, wp.box_lo_y + br), wp.box_hi_y - br);
+      p.x = fminf(fmaxf(p.x, wp.box_lo_x + k.br), wp.box_hi_x - k.br);
+      p.y = fminf(fmaxf(p.y, wp.box_lo_y + k.br), wp.box_hi_y - k.br);
     }
-    a_out[j] = make_float4(snap.x, snap.y, r, a.w);
-    b_out[j] = make_float4(p.x, p.y, po.x, po.y);
-    v_out[j] = vel;
-    if (args.do_keys) {
+    a.a_out[j] = make_float4(snap.x, snap.y, r, av.w);
+    a.b_out[j] = make_float4(p.x, p.y, po.x, po.y);
+    if (a.springs || a.write_v) a.v_out[j] = vel;
+    if (a.do_keys) {
       const uint32_t key = cell_key(wp, snap);
       w.key[j] = key;
       w.rank[j] = atomicAdd(w.cell_count + key, 1u);
     }
   }
-  if (CONTACTS) count_warp(w, ncontacts, npush);
+  if (a.contacts) count_warp(w, ncontacts, npush);
 }
 
 // Keys and ranks of the current storage (after a load or a host write).
-template <bool MW>
-__global__ void __launch_bounds__(256) k_keys_single(WorldDev w, const float4* __restrict__ A) {
+__global__ void __launch_bounds__(256) k_keys_single(WorldDev w, const float4* __restrict__ A, int mode) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= w.n_bodies) return;
   const float4 a = A[j];
   const uint32_t c = __float_as_uint(a.w);
-  const WorldParam wp = w.wparam[MW ? rec_world(w.body_c[c < w.n_bodies ? c : 0u]) : 0u];
-  const uint32_t key = cell_key(wp, v2(a.x, a.y));
+  const uint32_t world = mode == 2 ? rec_world(w.body_c[c < w.n_bodies ? c : 0u]) : 0u;
+  const uint32_t key = cell_key(w.wparam[world], v2(a.x, a.y));
   w.key[j] = key;
   w.rank[j] = atomicAdd(w.cell_count + key, 1u);
 }
@@ -409,9 +512,9 @@ __global__ void __launch_bounds__(256) k_gather_single(WorldDev w, const float4*
   if (pos) pos[c] = v2(b.x, b.y);
   if (pos_old) pos_old[c] = v2(b.z, b.w);
   if (vel) {
-    const float2 v = V[j];
-    // V holds the displacement of the last substep when v_div != 0 (static
+    // V holds the last substep's displacement when v_div != 0 (static
     // bodies store 0, and 0 / dt = 0)
+    const float2 v = V[j];
     vel[c] = v_div != 0.0f ? divs(v, v_div) : v;
   }
   if (snap) snap[c] = v2(a.x, a.y);
@@ -442,71 +545,42 @@ __global__ void __launch_bounds__(256) k_write_single(WorldDev w, const float4* 
   if (vel) V[j] = vel[c];
 }
 
-__global__ void __launch_bounds__(256) k_where_single(WorldDev w, const float4* __restrict__ A) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= w.n_bodies) return;
-  const uint32_t c = __float_as_uint(A[j].w);
-  if (c < w.n_bodies) w.where[c] = j;
-}
-
 // ---------------------------------------------------------------------------
 static inline uint32_t nblocks(uint32_t n) { return (n + 255u) / 256u; }
 
-void launch_permute(const WorldDev& w, int from, bool springs, cudaStream_t st) {
+void launch_permute(const WorldDev& w, const SingleArgs& a, cudaStream_t st) {
   if (!w.n_bodies) return;
-  const int to = from ^ 1;
-  if (springs)
-    k_permute<true><<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[from], w.sb[from], w.sv[from], w.sa[to], w.sb[to],
-                                                         w.sv[to]);
-  else
-    k_permute<false><<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[from], w.sb[from], w.sv[from], w.sa[to],
-                                                          w.sb[to], w.sv[to]);
+  k_permute<<<nblocks(w.n_bodies), 256, 0, st>>>(w, a);
 }
 
-#define BLOBS_B(v, NAME, ...) \
-  if (v) {                    \
-    constexpr bool NAME = true; \
-    __VA_ARGS__;              \
-  } else {                    \
-    constexpr bool NAME = false; \
-    __VA_ARGS__;              \
-  }
-
-void launch_step_single(const WorldDev& w, int from, int to, bool mw, bool springs, bool pending, bool contacts,
-                        float dt, float old_dt, bool do_keys, bool rot_dynamic, cudaStream_t st) {
+void launch_scatter_cand(const WorldDev& w, const float4* a_in, float4* cand, cudaStream_t st) {
   if (!w.n_bodies) return;
-  SubstepArgs a{dt, old_dt, dt / old_dt, dt / dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
+  k_scatter_cand<<<nblocks(w.n_bodies), 256, 0, st>>>(w, a_in, cand);
+}
+
+void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st) {
+  if (!w.n_bodies) return;
   const uint32_t g = nblocks(w.n_bodies);
-  BLOBS_B(mw, MW,
-    BLOBS_B(springs, SP,
-      BLOBS_B(pending, PE,
-        BLOBS_B(contacts, CO,
-          k_step_single<MW, SP, PE, CO><<<g, 256, 0, st>>>(w, w.sa[from], w.sb[from], w.sv[from], w.sa[to],
-                                                          w.sb[to], w.sv[to], a)))));
+  if (mode == 0) k_step_single<0><<<g, 256, 0, st>>>(w, a);
+  else if (mode == 1) k_step_single<1><<<g, 256, 0, st>>>(w, a);
+  else k_step_single<2><<<g, 256, 0, st>>>(w, a);
 }
 
-void launch_keys_single(const WorldDev& w, int cur, bool mw, cudaStream_t st) {
+void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st) {
   if (!w.n_bodies) return;
-  if (mw) k_keys_single<true><<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[cur]);
-  else k_keys_single<false><<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[cur]);
+  k_keys_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, mode);
 }
 
-void launch_gather_single(const WorldDev& w, int cur, float2* pos, float2* pos_old, float2* vel, float2* snap,
-                          float v_div, cudaStream_t st) {
+void launch_gather_single(const WorldDev& w, const float4* A, const float4* B, const float2* V, float2* pos,
+                          float2* pos_old, float2* vel, float2* snap, float v_div, cudaStream_t st) {
   if (!w.n_bodies) return;
-  k_gather_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[cur], w.sb[cur], w.sv[cur], pos, pos_old, vel, snap,
-                                                       v_div);
+  k_gather_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, B, V, pos, pos_old, vel, snap, v_div);
 }
 
-void launch_write_single(const WorldDev& w, int cur, const float2* pos, const float2* pos_old, const float2* vel,
-                         cudaStream_t st) {
+void launch_write_single(const WorldDev& w, const float4* A, float4* B, float2* V, const float2* pos,
+                         const float2* pos_old, const float2* vel, cudaStream_t st) {
   if (!w.n_bodies) return;
-  k_write_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[cur], w.sb[cur], w.sv[cur], pos, pos_old, vel);
-}
-
-void launch_where_single(const WorldDev& w, int cur, cudaStream_t st) {
-  if (!w.n_bodies) return;
-  k_where_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, w.sa[cur]);
+  k_write_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, B, V, pos, pos_old, vel);
 }
 
 }  // namespace blobs

@@ -11,7 +11,7 @@
 #include <map>
 #include <vector>
 
-#include "../../include/blobs_gpu.h"
+#include "blobs_gpu.h"
 #include "device.cuh"
 #include "kernels.h"
 #include "world.h"
@@ -114,7 +114,9 @@ struct blobs_world {
   bool multiworld = false, single = false, has_springs = false, has_joints = false, rot_dynamic = false;
   bool any_dynamic = false;
   bool sorted_storage = false;  // single-sphere path: body state in cell-sorted storage (single.cu)
-  float v_div = 0.0f;           // sorted storage without springs: V holds disp of a substep of this dt
+  int single_mode = 1;          // 0: one uniform world, 1: one world, 2: batched (single.cu)
+  float v_div = 0.0f;           // sorted storage without springs: V[vbuf] holds the displacement of a substep of this dt
+  int vbuf = 0;                 // sorted storage without springs: the V buffer in use
   bool pending = false;
   bool keys_valid = false;
   std::vector<uint32_t> colour_offsets;  // colour k = joints [colour_offsets[k], colour_offsets[k+1]) in processing order
@@ -129,6 +131,7 @@ struct blobs_world {
   WorldDev dev{};
   uint32_t sticky_status = 0;
   std::map<GraphKey, cudaGraphExec_t> graphs;
+  std::map<GraphKey, uint32_t> graph_cur_after;  // storage buffer holding the state after the graph
   cudaStream_t user_stream = nullptr;  // caller's stream (NULL: the world's own)
   bool timing = false;
   bool capturing = false;
@@ -147,6 +150,7 @@ struct blobs_world {
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+    graph_cur_after.clear();
     for (auto& kv : graph_timing) kv.second.destroy();
     graph_timing.clear();
     eager_timing.destroy();
@@ -419,6 +423,12 @@ int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h
     // the rounding of v / cs for coordinates up to ~1e5 cells.
     const float safe = rmax > 0.0f ? 2.0f * rmax * (1.0f + 1.0f / 64.0f) : 1.0f;
     const float cs = cfg.cell_size > safe ? cfg.cell_size : safe;
+    if (s.world_box) {  // bodies stay inside the walls: grid the whole box
+      lo_x = std::min(lo_x, s.world_box[4 * w + 0]);
+      lo_y = std::min(lo_y, s.world_box[4 * w + 1]);
+      hi_x = std::max(hi_x, s.world_box[4 * w + 2]);
+      hi_y = std::max(hi_y, s.world_box[4 * w + 3]);
+    }
     const double ex = hi_x >= lo_x ? (double)hi_x - lo_x : 0.0, ey = hi_y >= lo_y ? (double)hi_y - lo_y : 0.0;
     uint32_t W = next_pow2(std::max<uint64_t>(4, (uint64_t)std::ceil(ex / cs) + 3));
     uint32_t H = next_pow2(std::max<uint64_t>(4, (uint64_t)std::ceil(ey / cs) + 3));
@@ -435,6 +445,10 @@ int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h
     wp.log2h = ilog2(H);
     wp.cs = cs;
     wp.inv_cs = 1.0f / cs;
+    // one empty cell column / row before the extent, so the world's cells
+    // are 1 .. W-2 and a 3x3 search inside it never wraps
+    wp.ox = std::isfinite(lo_x) ? lo_x - cs : 0.0f;
+    wp.oy = std::isfinite(lo_y) ? lo_y - cs : 0.0f;
     if (s.world_box) {
       wp.has_box = 1;
       wp.box_lo_x = s.world_box[4 * w + 0];
@@ -464,6 +478,7 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t 
   d.sb[1] = cv.take<float4>(ss);
   d.sv[0] = cv.take<float2>(ss);
   d.sv[1] = cv.take<float2>(ss);
+  d.cand = cv.take<float4>(ss);
   d.body_c = cv.take<float4>(ss);
   d.key = cv.take<uint32_t>(ss);
   d.ckey = cv.take<uint32_t>(ss);
@@ -543,7 +558,7 @@ void mark_end(blobs_world* w) {
   else cudaEventRecord(b, w->st());
 }
 
-void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
+void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool first_in_step, bool last_in_step) {
   const WorldDev& d = w->dev;
   float2* in = w->pos[w->cur];
   float2* out = w->pos[w->cur ^ 1u];
@@ -558,35 +573,66 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
     w->enqueued += (uint64_t)w->cfg.joint_iterations * n_colours;
   };
   if (w->sorted_storage) {
+    // the first substep of a step re-sorts the body storage into cell order;
+    // the others only scatter a cell-order copy of the snapshot records
     const int cur = (int)w->cur;
+    SingleArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.dt = dt;
+    a.ratio_first = dt / old_dt;
+    a.ratio_rest = dt / dt;
+    a.pending = pending ? 1u : 0u;
+    a.springs = w->has_springs ? 1u : 0u;
+    a.rot_dynamic = w->rot_dynamic ? 1u : 0u;
+    a.write_v = last_in_step ? 1u : 0u;
+    a.move_v = w->has_springs ? 1u : 0u;
+    int in = cur, out = cur ^ 1;
     if (coll) {
       if (!w->keys_valid) {
-        launch_keys_single(d, cur, w->multiworld, st);
+        launch_keys_single(d, d.sa[cur], w->single_mode, st);
         w->enqueued += 1;
       }
       mark_begin(w, PHASE_SCAN);
       launch_scan(d, st);
       mark_end(w);
       mark_begin(w, PHASE_SCATTER);
-      launch_permute(d, cur, w->has_springs, st);
+      if (first_in_step) {
+        a.a_in = d.sa[cur];
+        a.b_in = d.sb[cur];
+        a.v_in = d.sv[cur];
+        a.a_out = d.sa[cur ^ 1];
+        a.b_out = d.sb[cur ^ 1];
+        a.v_out = d.sv[cur ^ 1];
+        launch_permute(d, a, st);
+        in = cur ^ 1;
+        out = cur;
+        a.cand = d.sa[in];
+        a.own_cell = d.ckey;
+      } else {
+        launch_scatter_cand(d, d.sa[cur], d.cand, st);
+        a.cand = d.cand;
+        a.own_cell = d.key;
+      }
       mark_end(w);
-      mark_begin(w, PHASE_CONTACT);
-      launch_step_single(d, cur ^ 1, cur, w->multiworld, w->has_springs, pending, true, dt, old_dt, true,
-                         w->rot_dynamic, st);
-      mark_end(w);
-      w->enqueued += 4;  // two scan kernels, permute, step
+      a.contacts = 1u;
+      a.do_keys = 1u;
+      w->enqueued += 4;  // two scan kernels, permute or scatter, step
       w->keys_valid = true;
-      w->v_div = w->has_springs ? 0.0f : dt;
     } else {
-      mark_begin(w, PHASE_INTEGRATE);
-      launch_step_single(d, cur, cur ^ 1, w->multiworld, w->has_springs, pending, false, dt, old_dt, false,
-                         w->rot_dynamic, st);
-      mark_end(w);
       w->enqueued += 1;
       w->keys_valid = false;
-      w->v_div = w->has_springs ? 0.0f : dt;
-      w->cur ^= 1u;
     }
+    a.a_in = d.sa[in];
+    a.b_in = d.sb[in];
+    a.v_in = d.sv[w->has_springs ? in : w->vbuf];
+    a.a_out = d.sa[out];
+    a.b_out = d.sb[out];
+    a.v_out = d.sv[w->has_springs ? out : w->vbuf];
+    mark_begin(w, coll ? PHASE_CONTACT : PHASE_INTEGRATE);
+    launch_step_single(d, a, w->single_mode, st);
+    mark_end(w);
+    w->cur = (uint32_t)out;
+    if (!w->has_springs && last_in_step) w->v_div = dt;
     return;
   }
   if (coll && !w->keys_valid) {
@@ -638,7 +684,7 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending) {
 void enqueue_integrate(blobs_world* w, float delta) {
   const float step_delta = delta / (float)w->cfg.substeps;
   for (uint32_t s = 0; s < w->cfg.substeps; ++s) {
-    enqueue_substep(w, step_delta, w->old_dt, w->pending);
+    enqueue_substep(w, step_delta, w->old_dt, w->pending, s == 0, s + 1 == w->cfg.substeps);
     w->pending = false;
     if (w->any_dynamic) w->old_dt = step_delta;
   }
@@ -656,11 +702,12 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
   const float step_delta = delta / (float)w->cfg.substeps;
   const bool coll = w->cfg.collisions_enabled && w->nc > 0;
   if (coll && !w->keys_valid) {
-    if (w->sorted_storage) launch_keys_single(w->dev, (int)w->cur, w->multiworld, w->st());
+    if (w->sorted_storage) launch_keys_single(w->dev, w->dev.sa[w->cur], w->single_mode, w->st());
     else launch_keys(w->dev, w->multiworld, w->st());
     w->keys_valid = true;
   }
-  GraphKey key{f2bits(delta), w->cur, n_steps, w->timing ? 1u : 0u};
+  // the buffers baked into a graph depend on where the state is now
+  GraphKey key{f2bits(delta), w->cur | ((uint32_t)w->vbuf << 1), n_steps, w->timing ? 1u : 0u};
   auto it = w->graphs.find(key);
   const uint32_t cur0 = w->cur;
   if (it == w->graphs.end()) {
@@ -671,10 +718,12 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
     w->recording = w->timing ? &w->graph_timing[key] : nullptr;
     const uint64_t before = w->enqueued;
     for (uint32_t n = 0; n < n_steps; ++n)
-      for (uint32_t s = 0; s < w->cfg.substeps; ++s) enqueue_substep(w, step_delta, step_delta, false);
+      for (uint32_t s = 0; s < w->cfg.substeps; ++s)
+        enqueue_substep(w, step_delta, step_delta, false, s == 0, s + 1 == w->cfg.substeps);
     w->capturing = false;
     w->recording = nullptr;
     w->graph_kernels[key] = w->enqueued - before;
+    w->graph_cur_after[key] = w->cur;
     w->enqueued = before;
     e = cudaStreamEndCapture(w->st(), &g);
     if (e != cudaSuccess) return blobs_map_cuda(e);
@@ -693,10 +742,8 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
     if (std::find(w->launched_sets.begin(), w->launched_sets.end(), ts) == w->launched_sets.end())
       w->launched_sets.push_back(ts);
   }
-  // the sorted-storage path returns to its buffer every substep with contacts
-  const bool flips = !(w->sorted_storage && coll);
-  w->cur = flips ? (cur0 ^ ((n_steps * w->cfg.substeps) & 1u)) : cur0;
-  if (w->sorted_storage) w->v_div = w->has_springs ? 0.0f : step_delta;
+  w->cur = w->graph_cur_after[key];
+  if (w->sorted_storage && !w->has_springs) w->v_div = step_delta;
   w->keys_valid = coll;
   return BLOBS_OK;
 }
@@ -854,6 +901,19 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   Counters* counters = nullptr;
   Carver sizer;
   const bool sorted_storage = h.single && nj == 0;
+  // a uniform single-sphere world needs no per-body constant record
+  bool uniform = sorted_storage && nw == 1;
+  uint32_t first_dyn = 0xffffffffu;
+  for (uint32_t i = 0; i < nb && uniform; ++i) {
+    if (h.bflags[i] & BF_STATIC) uniform = false;
+    if (h.gmod[i] != h.gmod[0] || std::isnan(h.gmod[i])) uniform = false;
+    if (!(h.mass[i] == h.col_radius[i] * 4.0f) || !(h.bound_r[i] == h.col_radius[i])) uniform = false;
+    if ((h.bflags[i] & BF_FIRST_DYN) && first_dyn == 0xffffffffu) first_dyn = i;
+  }
+  if (!h.wparam.empty()) {
+    h.wparam[0].first_dyn = first_dyn;
+    h.wparam[0].uniform_gmod = nb ? h.gmod[0] : 1.0f;
+  }
   carve(sizer, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   e = cudaMalloc(&w->arena, sizer.off + 256);
   if (e != cudaSuccess) return blobs_map_cuda(e);
@@ -963,7 +1023,9 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   w->multiworld = nw > 1;
   w->single = h.single;
   w->sorted_storage = sorted_storage;
+  w->single_mode = nw > 1 ? 2 : (uniform ? 0 : 1);
   w->v_div = 0.0f;
+  w->vbuf = 0;
   w->has_springs = ns > 0;
   w->has_joints = nj > 0;
   w->rot_dynamic = h.rot_dynamic;
@@ -1025,8 +1087,10 @@ int blobs_world_read_bodies(blobs_world* w, float* pos, float* pos_old, float* v
   cudaStream_t s = w->st();
   if (w->sorted_storage) {
     // storage order -> arena order into the staging arrays, then copy out
-    launch_gather_single(w->dev, (int)w->cur, pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr,
-                         vel ? w->dev.vel : nullptr, nullptr, w->v_div, s);
+    const int c = (int)w->cur;
+    launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf],
+                         pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr,
+                         nullptr, w->v_div, s);
     e = cudaGetLastError();
     if (e == cudaSuccess && pos && n) e = cudaMemcpyAsync(pos, w->pos[0], n * 8, cudaMemcpyDeviceToHost, s);
   } else if (pos && n) {
@@ -1047,7 +1111,9 @@ int blobs_world_read_snapshots(blobs_world* w, float* xy) {
   cudaSetDevice(w->cfg.device);
   cudaError_t e = cudaSuccess;
   if (w->sorted_storage) {
-    launch_gather_single(w->dev, (int)w->cur, nullptr, nullptr, nullptr, w->dev.snap, 0.0f, w->st());
+    const int c = (int)w->cur;
+    launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[0], nullptr, nullptr, nullptr, w->dev.snap,
+                         0.0f, w->st());
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && w->nc) e = cudaMemcpyAsync(xy, w->dev.snap, (size_t)w->nc * 8, cudaMemcpyDeviceToHost, w->st());
@@ -1114,8 +1180,9 @@ int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_
   if (e == cudaSuccess && vel && n) e = cudaMemcpyAsync(w->dev.vel, vel, n * 8, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && w->sorted_storage && n) {
     // arena order staging -> storage order
-    launch_write_single(w->dev, (int)w->cur, pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr,
-                        vel ? w->dev.vel : nullptr, s);
+    const int c = (int)w->cur;
+    launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf],
+                        pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr, s);
     if (vel) w->v_div = 0.0f;  // every V entry is now a velocity
     e = cudaGetLastError();
   }
@@ -1142,10 +1209,23 @@ int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, u
   // recomputes its ranks (the scan consumed the counts)
   WorldDev dv = w->dev;
   if (w->sorted_storage) {
-    if (!w->keys_valid) launch_keys_single(w->dev, (int)w->cur, w->multiworld, s);
+    const int c = (int)w->cur;
+    if (!w->keys_valid) launch_keys_single(w->dev, w->dev.sa[c], w->single_mode, s);
     launch_scan(w->dev, s);
-    launch_permute(w->dev, (int)w->cur, w->has_springs, s);
+    SingleArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.a_in = w->dev.sa[c];
+    a.b_in = w->dev.sb[c];
+    // V moves with the records; without springs it lives in its own buffer
+    const int vi = w->has_springs ? c : w->vbuf;
+    a.v_in = w->dev.sv[vi];
+    a.a_out = w->dev.sa[c ^ 1];
+    a.b_out = w->dev.sb[c ^ 1];
+    a.v_out = w->dev.sv[vi ^ 1];
+    a.move_v = 1u;
+    launch_permute(w->dev, a, s);
     w->cur ^= 1u;  // the permuted storage becomes current
+    if (!w->has_springs) w->vbuf ^= 1;
     dv.sorted = w->dev.sa[w->cur];
   } else {
     if (!w->keys_valid) launch_keys(w->dev, w->multiworld, s);
@@ -1177,8 +1257,8 @@ int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, u
   return total > cap ? BLOBS_ERR_OVERFLOW : BLOBS_OK;
 }
 
-int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, uint32_t* log2_width,
-                     uint32_t* log2_height) {
+int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, float* origin,
+                     uint32_t* log2_width, uint32_t* log2_height) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
   if (!w->loaded) return BLOBS_ERR_STATE;
   if (world >= w->nw) return BLOBS_ERR_INVALID_ARGUMENT;
@@ -1188,6 +1268,10 @@ int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* in
   if (e != cudaSuccess) return blobs_map_cuda(e);
   if (cell_size) *cell_size = wp.cs;
   if (inv_cell_size) *inv_cell_size = wp.inv_cs;
+  if (origin) {
+    origin[0] = wp.ox;
+    origin[1] = wp.oy;
+  }
   if (log2_width) *log2_width = wp.log2w;
   if (log2_height) *log2_height = wp.log2h;
   return BLOBS_OK;

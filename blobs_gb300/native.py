@@ -99,7 +99,7 @@ def lib() -> ctypes.CDLL:
         "blobs_world_write_bodies": (i32, [_P, _P, _P, _P, _P, _P]),
         "blobs_world_set_timing": (i32, [_P, i32]),
         "blobs_world_emit_pairs": (i32, [_P, i32, _P, u64, ctypes.POINTER(u64)]),
-        "blobs_world_grid": (i32, [_P, u32, ctypes.POINTER(f32), ctypes.POINTER(f32), ctypes.POINTER(u32),
+        "blobs_world_grid": (i32, [_P, u32, ctypes.POINTER(f32), ctypes.POINTER(f32), _P, ctypes.POINTER(u32),
                                    ctypes.POINTER(u32)]),
         "blobs_world_kernel_launches": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_phase_times": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(u64), u32]),
@@ -303,11 +303,12 @@ class World:
         return out[np.lexsort((out[:, 1], out[:, 0]))]
 
     def grid(self, world: int = 0):
-        """(cell size, f32 reciprocal, log2 width, log2 height) of a world's grid."""
+        """(cell size, f32 reciprocal, origin (2,), log2 width, log2 height) of a world's grid."""
         cs, inv, lw, lh = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32(), ctypes.c_uint32()
-        check(lib().blobs_world_grid(self._h, world, ctypes.byref(cs), ctypes.byref(inv), ctypes.byref(lw),
-                                     ctypes.byref(lh)), "grid")
-        return cs.value, inv.value, lw.value, lh.value
+        org = np.zeros(2, np.float32)
+        check(lib().blobs_world_grid(self._h, world, ctypes.byref(cs), ctypes.byref(inv), _ptr(org),
+                                     ctypes.byref(lw), ctypes.byref(lh)), "grid")
+        return cs.value, inv.value, org, lw.value, lh.value
 
     def kernel_launches(self) -> int:
         n = ctypes.c_uint64()

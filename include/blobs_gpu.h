@@ -219,10 +219,11 @@ int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
  * BLOBS_ERR_OVERFLOW with *n_pairs = the full count when cap is too small. */
 int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, uint64_t cap, uint64_t* n_pairs);
 /* The toroidal cell grid of world `world`: cell edge, its f32 reciprocal,
- * and log2 of the width and height in cells (cell (ix, iy) =
- * floor(v * inv_cell_size) wrapped mod 2^log2). */
-int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, uint32_t* log2_width,
-                     uint32_t* log2_height);
+ * the origin (2 floats) and log2 of the width and height in cells
+ * (cell (ix, iy) = floor((v - origin) * inv_cell_size) in f32, wrapped mod
+ * 2^log2). */
+int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* inv_cell_size, float* origin,
+                     uint32_t* log2_width, uint32_t* log2_height);
 /* Physics.time and the accumulator of fixed_step. */
 int blobs_world_time(blobs_world* w, double* time, double* accumulator);
 /* The joint processing order the GPU schedule uses (graph colouring: joints

@@ -17,11 +17,11 @@ def grid_coord(v, inv_cs):
     return np.clip(q, -2 ** 31, 2 ** 31 - 1).astype(np.int64)
 
 
-def cpu_candidates(snap, inv_cs, log2w, log2h):
+def cpu_candidates(snap, inv_cs, origin, log2w, log2h):
     """All (hi, lo) pairs whose wrapped cells are 3x3 neighbours."""
     W, H = 1 << log2w, 1 << log2h
-    ix = grid_coord(snap[:, 0], inv_cs) % W
-    iy = grid_coord(snap[:, 1], inv_cs) % H
+    ix = grid_coord(snap[:, 0].astype(np.float32) - np.float32(origin[0]), inv_cs) % W
+    iy = grid_coord(snap[:, 1].astype(np.float32) - np.float32(origin[1]), inv_cs) % H
     key = iy * W + ix
     order = np.argsort(key, kind="stable")
     buckets = {}
@@ -45,10 +45,10 @@ def test_candidate_pairs_bit_exact(n, literal):
     with native.World(s) as w:
         w.step(s.dt)
         snap = w.read_snapshots()
-        cs, inv_cs, lw, lh = w.grid()
+        cs, inv_cs, origin, lw, lh = w.grid()
         assert inv_cs == np.float32(1.0) / np.float32(cs)
         got = w.emit_pairs(contacts_only=False)
-    want = cpu_candidates(snap, inv_cs, lw, lh)
+    want = cpu_candidates(snap, inv_cs, origin, lw, lh)
     assert got.shape == want.shape and np.array_equal(got, want)
 
 
