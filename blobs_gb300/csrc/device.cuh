@@ -145,11 +145,16 @@ __device__ __host__ __forceinline__ int32_t cell_coord(float v, float cs) {
 // NaN -> 0.  Monotone in v; with cs >= 2 rmax (1 + 1/64) two spheres in
 // contact always land in 3x3-neighbouring cells for |v| / cs up to ~1e5.
 __device__ __host__ __forceinline__ int32_t grid_coord(float v, float inv_cs) {
+#ifdef __CUDA_ARCH__
+  // cvt.rmi.s32.f32: floor, saturating, NaN -> 0 -- the same function
+  return __float2int_rd(v * inv_cs);
+#else
   float q = floorf(v * inv_cs);
   if (q != q) return 0;
   if (q >= 2147483648.0f) return 2147483647;
   if (q <= -2147483648.0f) return (-2147483647 - 1);
   return (int32_t)q;
+#endif
 }
 
 // Global cell index of a point in world `wp`'s toroidal grid:

@@ -82,20 +82,20 @@ __device__ __forceinline__ uint32_t slot_of(const Segments& g, uint32_t t) {
 // `en`, loads issued together for memory-level parallelism.
 __device__ __forceinline__ bool near_pair(float dx, float dy, float mind);
 
-__device__ __forceinline__ void near_range(const float4* __restrict__ C, float2 s, float r, uint32_t st, uint32_t en,
-                                           uint32_t& t, unsigned long long& near) {
+__device__ __forceinline__ void near_range(const float4* __restrict__ C, float2 s, float r, uint32_t self,
+                                           uint32_t st, uint32_t en, uint32_t& t, unsigned long long& near) {
   for (uint32_t q = st; q < en; q += 4u, t += 4u) {
     const float4 far = make_float4(3.0e38f, 3.0e38f, 0.0f, 0.0f);
     const float4 o0 = C[q];
     const float4 o1 = q + 1u < en ? C[q + 1u] : far;
     const float4 o2 = q + 2u < en ? C[q + 2u] : far;
     const float4 o3 = q + 3u < en ? C[q + 3u] : far;
-    unsigned long long m = 0ull;
-    if (near_pair(s.x - o0.x, s.y - o0.y, r + o0.z)) m |= 1ull;
-    if (near_pair(s.x - o1.x, s.y - o1.y, r + o1.z)) m |= 2ull;
-    if (near_pair(s.x - o2.x, s.y - o2.y, r + o2.z)) m |= 4ull;
-    if (near_pair(s.x - o3.x, s.y - o3.y, r + o3.z)) m |= 8ull;
-    near |= m << t;
+    uint32_t m = 0u;
+    if (near_pair(s.x - o0.x, s.y - o0.y, r + o0.z) && __float_as_uint(o0.w) != self) m |= 1u;
+    if (near_pair(s.x - o1.x, s.y - o1.y, r + o1.z) && __float_as_uint(o1.w) != self) m |= 2u;
+    if (near_pair(s.x - o2.x, s.y - o2.y, r + o2.z) && __float_as_uint(o2.w) != self) m |= 4u;
+    if (near_pair(s.x - o3.x, s.y - o3.y, r + o3.z) && __float_as_uint(o3.w) != self) m |= 8u;
+    if (m) near |= (unsigned long long)m << t;
   }
 }
 
@@ -317,13 +317,14 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
         // (row 0 at bit 0, row 1 at bit 4*ceil(l0/4), ...).
         unsigned long long near = 0ull;
         uint32_t t = 0;
-        near_range(C, s, r, s0, s0 + l0, t, near);
+        near_range(C, s, r, c, s0, s0 + l0, t, near);
         const uint32_t t1 = t;
-        near_range(C, s, r, s1, s1 + l1, t, near);
+        near_range(C, s, r, c, s1, s1 + l1, t, near);
         const uint32_t t2 = t;
-        near_range(C, s, r, s2, s2 + l2, t, near);
+        near_range(C, s, r, c, s2, s2 + l2, t, near);
         // Phase 2: the near candidates in ascending arena id (the
         // reference's pair order for this body), the warp's lanes in step.
+        // One near candidate needs no ordering.
         while (near) {
           unsigned long long best_bit = 0ull;
           uint32_t best = 0xffffffffu;
@@ -338,6 +339,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
               bo = o;
               best_bit = mk & (~mk + 1ull);
             }
+            if ((near & (near - 1ull)) == 0ull) break;
           }
           near &= ~best_bit;
           if (best >= w.n_bodies || best == c) continue;
