@@ -230,6 +230,35 @@ int blobs_world_time(blobs_world* w, double* time, double* accumulator);
  * sorted by colour, then by arena index).  `order` holds n_joints entries. */
 int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours);
 
+/* ---- contact pairs without any allocation ------------------------------------ */
+
+/* No counterpart in the reference.  The contact pair set of
+ * blobs_world_emit_pairs(contacts_only = 1) -- pairs (hi, lo), hi > lo, with
+ * different parents, passing InteractionGroups::test and closer than the sum
+ * of their radii -- for `n` colliders already in device memory, computed
+ * without a world and without allocating: for hosts that must not call
+ * cudaMalloc / cudaFree while they run (those calls synchronise the whole
+ * device, which a frame loop cannot absorb) or whose device memory belongs to
+ * their own budgeted allocator.  All scratch lives in one static device array
+ * of this library sized for at most blobs_noalloc_max_colliders() (65,536)
+ * colliders; every GPU that loads the library holds it (about 2.3 MB) until
+ * the process exits.  Larger n is rejected with BLOBS_ERR_INVALID_ARGUMENT.
+ *   snap: 2n floats (device), radius: n floats (device); parent / memb / filt:
+ *   n uint32 (device) or NULL (all different / all groups);
+ *   pairs: 2 * cap uint32 (device); count: one device counter that receives
+ *   the full number of pairs (pairs past `cap` are counted, not written).
+ * Asynchronous on `stream` (a cudaStream_t, NULL = the legacy default).  The
+ * first call on a device looks up the device address of the scratch array
+ * (once, with that device current); make that first call before any stream
+ * capture.  Every call reuses the same scratch array, so calls whose work
+ * overlaps on the GPU race: issue them on one stream, or wait for the
+ * previous one. */
+int blobs_contact_pairs_noalloc(uint32_t n, const float* snap, const float* radius, const uint32_t* parent,
+                                const uint32_t* memb, const uint32_t* filt, uint32_t* pairs, uint64_t cap,
+                                unsigned long long* count, void* stream);
+/* The largest collider count blobs_contact_pairs_noalloc accepts. */
+uint32_t blobs_noalloc_max_colliders(void);
+
 /* ---- host-side helpers (no device needed) ---------------------------------- */
 
 /* RigidBody::update_mass_and_inertia (rigid_body.rs:96-128) for every body,
