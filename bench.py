@@ -181,6 +181,59 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def batched_comparison(dev, steps=100, sample=256, seed=4):
+    """Configuration 4: 4,096 uneven worlds stepped as one batch (a 100-step
+    rollout captured in one CUDA graph) against the per-world form (each
+    world its own device world and its own 100-step rollout launch), timed on
+    `sample` evenly spaced worlds and scaled to all 4,096 by body count."""
+    import numpy as np
+    import torch
+    from blobs_gb300 import native, scenes
+    scene = scenes.config4(seed=seed, steps=steps)
+    dt = scene.dt
+    stream = torch.cuda.current_stream(dev)
+    w = native.World(scene, device=dev.index)
+    w.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        w.step(dt)
+    w.rollout(dt, steps)  # capture
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    w.rollout(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1)
+    w.sync()
+    w.close()
+    idx = np.linspace(0, scene.n_worlds - 1, sample).astype(int)
+    worlds, bodies = [], 0
+    for i in idx:
+        sub = scenes.unpack_world(scene, int(i))
+        ww = native.World(sub, device=dev.index)
+        ww.set_stream(stream.cuda_stream)
+        for _ in range(3):
+            ww.step(dt)
+        ww.rollout(dt, steps)  # capture
+        worlds.append(ww)
+        bodies += sub.n_bodies
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for ww in worlds:
+        ww.rollout(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sample_ms = e0.elapsed_time(e1)
+    for ww in worlds:
+        ww.close()
+    per_world_ms = sample_ms * scene.n_bodies / bodies
+    return {"worlds": scene.n_worlds, "bodies": scene.n_bodies, "steps": steps,
+            "batched_ms": batched_ms, "per_world_ms_est": per_world_ms, "speedup": per_world_ms / batched_ms,
+            "batched_sphere_steps_per_s": scene.n_bodies * steps / (batched_ms / 1e3),
+            "sample": "%d evenly spaced worlds (%d bodies) run one rollout launch per world, scaled by body count"
+                      % (sample, bodies)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -300,6 +353,9 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(target_n=scene.n_bodies)
+    if rank == 0 and not args.no_batched:
+        world.close()
+        line["batched"] = batched_comparison(dev)
     world.close()
     if dist is not None:
         dist.barrier()
@@ -316,6 +372,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
