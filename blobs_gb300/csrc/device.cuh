@@ -196,6 +196,11 @@ struct SingleArgs {
   const uint32_t* own_cell;  // cell of each storage slot in this substep's order
   float dt, ratio_first, ratio_rest;
   uint32_t contacts, pending, springs, rot_dynamic, do_keys, write_v, move_v;
+  // contact recording for the adjoint (NULL in ordinary steps): pairs
+  // (hi, lo | pushed << 31) in arena ids
+  uint2* rec_pairs;
+  uint32_t* rec_count;
+  uint32_t rec_cap;
 };
 
 constexpr int SCAN_THREADS = 256;

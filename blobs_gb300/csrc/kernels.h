@@ -28,7 +28,38 @@ void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaSt
 void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st);
 void launch_gather_single(const WorldDev& w, const float4* A, const float4* B, const float2* V, float2* pos,
                           float2* pos_old, float2* vel, float2* snap, float v_div, cudaStream_t st);
-void launch_write_single(const WorldDev& w, const float4* A, float4* B, float2* V, const float2* pos,
-                         const float2* pos_old, const float2* vel, cudaStream_t st);
+void launch_write_single(const WorldDev& w, float4* A, float4* B, float2* V, const float2* pos,
+                         const float2* pos_old, const float2* vel, const float2* snap, cudaStream_t st);
+
+// adjoint of the single-sphere substep (adjoint.cu)
+struct AdjointSubstep {
+  // recorded state at the start of the substep (t) and after it (t + 1), arena order
+  const float2* p_t;
+  const float2* s_t;
+  const float2* v_t;
+  const float2* p_t1;
+  const float2* s_t1;
+  const uint2* pairs;      // contacts resolved in the substep (hi, lo | pushed << 31)
+  const uint32_t* n_pairs;
+  // adjoints of the state after the substep (in) and before it (out)
+  const float2* lp_in;
+  const float2* lpo_in;
+  const float2* ls_in;
+  const float2* lv_in;
+  float2* lp_out;
+  float2* lpo_out;
+  float2* ls_out;
+  float2* lv_out;
+  float2* lpc;             // scratch: adjoint of the post-contact position
+  float2* la;              // scratch: adjoint of the acceleration
+  float2* lv0;             // gradient of the velocity requests (first substep of the rollout)
+  float* lk;               // gradient of the spring stiffnesses (accumulated)
+  float dt;
+  float ratio_first;       // dt / old_dt for the first dynamic body (first substep only)
+  uint32_t first_substep;  // the rollout's first substep (dt / old_dt applies)
+  uint32_t vreq_pending;   // velocity requests were pending at the rollout's start
+  uint32_t pair_cap;
+};
+void launch_adjoint_substep(const WorldDev& w, const AdjointSubstep& a, cudaStream_t st);
 
 }  // namespace blobs

@@ -153,6 +153,12 @@ __device__ __forceinline__ bool single_pair(const WorldDev& w, const SingleArgs&
   return true;
 }
 
+// Append a resolved contact (arena ids, hi > lo) for the adjoint pass.
+__device__ __forceinline__ void record_pair(const SingleArgs& a, uint32_t hi, uint32_t lo, bool pushed) {
+  const uint32_t k = atomicAdd(a.rec_count, 1u);
+  if (k < a.rec_cap) a.rec_pairs[k] = make_uint2(hi, lo | (pushed ? 0x80000000u : 0u));
+}
+
 __device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush) {
   uint32_t t = ncontacts, p = npush;
 #pragma unroll
@@ -235,6 +241,7 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
     if (best < c) {
       ++ncontacts;
       npush += sp.pushed ? 1u : 0u;
+      if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
     }
     last = best;
     first = false;
@@ -351,6 +358,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
+            if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
           }
         }
       } else {
@@ -400,6 +408,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
+            if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
           }
         }
       } else {
@@ -522,9 +531,9 @@ __global__ void __launch_bounds__(256) k_gather_single(WorldDev w, const float4*
   if (snap) snap[c] = v2(a.x, a.y);
 }
 
-__global__ void __launch_bounds__(256) k_write_single(WorldDev w, const float4* __restrict__ A, float4* B,
-                                                      float2* V, const float2* pos, const float2* pos_old,
-                                                      const float2* vel) {
+__global__ void __launch_bounds__(256) k_write_single(WorldDev w, float4* A, float4* B, float2* V,
+                                                      const float2* pos, const float2* pos_old, const float2* vel,
+                                                      const float2* snap) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= w.n_bodies) return;
   const uint32_t c = __float_as_uint(A[j].w);
@@ -545,6 +554,11 @@ __global__ void __launch_bounds__(256) k_write_single(WorldDev w, const float4* 
   }
   B[j] = b;
   if (vel) V[j] = vel[c];
+  if (snap) {
+    const float2 q = snap[c];
+    A[j].x = q.x;
+    A[j].y = q.y;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -579,10 +593,10 @@ void launch_gather_single(const WorldDev& w, const float4* A, const float4* B, c
   k_gather_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, B, V, pos, pos_old, vel, snap, v_div);
 }
 
-void launch_write_single(const WorldDev& w, const float4* A, float4* B, float2* V, const float2* pos,
-                         const float2* pos_old, const float2* vel, cudaStream_t st) {
+void launch_write_single(const WorldDev& w, float4* A, float4* B, float2* V, const float2* pos,
+                         const float2* pos_old, const float2* vel, const float2* snap, cudaStream_t st) {
   if (!w.n_bodies) return;
-  k_write_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, B, V, pos, pos_old, vel);
+  k_write_single<<<nblocks(w.n_bodies), 256, 0, st>>>(w, A, B, V, pos, pos_old, vel, snap);
 }
 
 }  // namespace blobs

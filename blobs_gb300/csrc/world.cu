@@ -134,6 +134,19 @@ struct blobs_world {
   std::map<GraphKey, uint32_t> graph_cur_after;  // storage buffer holding the state after the graph
   cudaStream_t user_stream = nullptr;  // caller's stream (NULL: the world's own)
   bool timing = false;
+  // contact recording of the eager path (adjoint recomputation)
+  uint2* rec_pairs = nullptr;
+  uint32_t* rec_count = nullptr;
+  uint32_t rec_cap = 0;
+  // differentiable rollout: checkpoints of the arena-order state
+  struct Recording {
+    bool valid = false;
+    double delta = 0.0;
+    uint32_t n_steps = 0, every = 0, n_seg = 0;
+    float old_dt0 = 1.0f;
+    bool pending0 = false;
+    float2* ckpt = nullptr;  // (n_seg + 1) x 4 x n_bodies float2: p, po, s, v
+  } rec;
   bool capturing = false;
   TimingSet* recording = nullptr;      // set that enqueue_substep records into
   std::map<GraphKey, TimingSet> graph_timing;
@@ -158,6 +171,8 @@ struct blobs_world {
   }
   void release() {
     drop_graphs();
+    if (rec.ckpt) cudaFree(rec.ckpt);
+    rec = Recording();
     if (arena) cudaFree(arena);
     arena = nullptr;
     if (hcounters) cudaFreeHost(hcounters);
@@ -586,6 +601,9 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.rot_dynamic = w->rot_dynamic ? 1u : 0u;
     a.write_v = last_in_step ? 1u : 0u;
     a.move_v = w->has_springs ? 1u : 0u;
+    a.rec_pairs = w->rec_pairs;
+    a.rec_count = w->rec_count;
+    a.rec_cap = w->rec_cap;
     int in = cur, out = cur ^ 1;
     if (coll) {
       if (!w->keys_valid) {
@@ -777,6 +795,24 @@ int run_steps(blobs_world* w, double delta, uint32_t n_steps) {
   }
   e = cudaGetLastError();
   return blobs_map_cuda(e);
+}
+
+// Arena-order state (p, po, s, v) of a single-sphere world into four
+// n-body float2 slices (v only holds velocities in worlds with springs).
+void gather_state(blobs_world* w, float2* p, float2* po, float2* sn, float2* v) {
+  const int c = (int)w->cur;
+  launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf], p, po,
+                       w->has_springs ? v : nullptr, sn, 0.0f, w->st());
+}
+
+void restore_state(blobs_world* w, const float2* p, const float2* po, const float2* sn, const float2* v) {
+  const int c = (int)w->cur;
+  launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf], p, po,
+                      w->has_springs ? v : nullptr, sn, w->st());
+  // the snapshots changed: the next substep recounts the cells from zero
+  cudaMemsetAsync(w->dev.cell_count, 0, sizeof(uint32_t) * (size_t)w->dev.n_cells, w->st());
+  w->keys_valid = false;
+  w->v_div = 0.0f;
 }
 
 int read_status(blobs_world* w) {
@@ -1182,7 +1218,8 @@ int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_
     // arena order staging -> storage order
     const int c = (int)w->cur;
     launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf],
-                        pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr, s);
+                        pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr,
+                        nullptr, s);
     if (vel) w->v_div = 0.0f;  // every V entry is now a velocity
     e = cudaGetLastError();
   }
@@ -1275,6 +1312,186 @@ int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* in
   if (log2_width) *log2_width = wp.log2w;
   if (log2_height) *log2_height = wp.log2h;
   return BLOBS_OK;
+}
+
+int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, uint32_t checkpoint_every) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  if (!w->sorted_storage || w->ncirc || n_steps == 0 || checkpoint_every == 0) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  auto& r = w->rec;
+  if (r.ckpt) cudaFree(r.ckpt);
+  r = blobs_world::Recording();
+  const uint32_t n_seg = (n_steps + checkpoint_every - 1) / checkpoint_every;
+  const size_t nb = w->nb;
+  cudaError_t e = cudaMalloc(&r.ckpt, sizeof(float2) * 4 * nb * (n_seg + 1));
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  if (w->has_springs) e = cudaMemsetAsync(r.ckpt, 0, sizeof(float2) * 4 * nb * (n_seg + 1), w->st());
+  r.delta = delta;
+  r.n_steps = n_steps;
+  r.every = checkpoint_every;
+  r.n_seg = n_seg;
+  r.old_dt0 = w->old_dt;
+  r.pending0 = w->pending;
+  for (uint32_t g = 0; g <= n_seg; ++g) {
+    float2* base = r.ckpt + 4 * nb * g;
+    gather_state(w, base, base + nb, base + 2 * nb, base + 3 * nb);
+    if (g == n_seg) break;
+    const uint32_t steps = std::min(checkpoint_every, n_steps - g * checkpoint_every);
+    int st = run_steps(w, delta, steps);
+    if (st) return st;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  r.valid = true;
+  return read_status(w);
+}
+
+int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded || !w->rec.valid) return BLOBS_ERR_STATE;
+  if (!dl_dpos) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(w->cfg.device);
+  auto& r = w->rec;
+  const size_t nb = w->nb;
+  const uint32_t S = r.every * w->cfg.substeps;  // substeps per full segment
+  const uint32_t cap = (uint32_t)std::min<size_t>(4 * nb + 1024, 0x7fffffffu);
+  cudaStream_t st = w->st();
+  // scratch of the reverse pass: sized by a first carve, then carved
+  const size_t slice = nb * sizeof(float2);
+  struct Scratch {
+    float2 *sp, *ss, *sv, *adj[2][4], *lpc, *la, *lv0;
+    uint2* pairs;
+    uint32_t* counts;
+    float* lk;
+    Counters* saved;
+  } x;
+  auto lay = [&](Carver& cv) {
+    x.sp = cv.take<float2>(nb * (S + 1));  // p, s, v of every recorded state
+    x.ss = cv.take<float2>(nb * (S + 1));
+    x.sv = cv.take<float2>(nb * (S + 1));
+    x.pairs = cv.take<uint2>((size_t)cap * S);  // contacts of every substep
+    x.counts = cv.take<uint32_t>(S);
+    for (int k = 0; k < 2; ++k)
+      for (int m = 0; m < 4; ++m) x.adj[k][m] = cv.take<float2>(nb);  // adjoints of (p, po, s, v) in / out
+    x.lpc = cv.take<float2>(nb);
+    x.la = cv.take<float2>(nb);
+    x.lv0 = cv.take<float2>(nb);
+    x.lk = cv.take<float>(w->ns ? w->ns : 1);
+    x.saved = cv.take<Counters>(1);
+  };
+  Carver sizer;
+  lay(sizer);
+  const size_t bytes = sizer.off;
+  char* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, bytes + 256);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  Carver cv;
+  cv.base = buf;
+  lay(cv);
+  float2* const sp = x.sp;
+  float2* const ss = x.ss;
+  float2* const sv = x.sv;
+  uint2* const pairs = x.pairs;
+  uint32_t* const counts = x.counts;
+  float2* const lpc = x.lpc;
+  float2* const la = x.la;
+  float2* const lv0 = x.lv0;
+  float* const lk = x.lk;
+  Counters* const saved = x.saved;
+  auto& adj = x.adj;
+  e = cudaMemsetAsync(buf, 0, bytes, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(saved, w->dcounters, sizeof(Counters), cudaMemcpyDeviceToDevice, st);
+  int in = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(adj[in][0], dl_dpos, slice, cudaMemcpyHostToDevice, st);
+  const float dt_sub = (float)r.delta / (float)w->cfg.substeps;
+  const bool saved_timing = w->timing;
+  w->timing = false;
+  int status = BLOBS_OK;
+  std::vector<uint32_t> hcounts(S);
+  for (int g = (int)r.n_seg - 1; g >= 0 && e == cudaSuccess && status == BLOBS_OK; --g) {
+    const uint32_t steps = std::min(r.every, r.n_steps - (uint32_t)g * r.every);
+    const uint32_t nsub = steps * w->cfg.substeps;
+    // restore the checkpoint and recompute the segment, recording every substep
+    const float2* ck = r.ckpt + 4 * nb * g;
+    restore_state(w, ck, ck + nb, ck + 2 * nb, ck + 3 * nb);
+    w->old_dt = g == 0 ? r.old_dt0 : dt_sub;
+    w->pending = g == 0 ? r.pending0 : false;
+    cudaMemcpyAsync(sp, ck, slice, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(ss, ck + 2 * nb, slice, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(sv, ck + 3 * nb, slice, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(counts, 0, sizeof(uint32_t) * S, st);
+    w->rec_cap = cap;
+    for (uint32_t t = 0; t < nsub; ++t) {
+      w->rec_pairs = pairs + (size_t)cap * t;
+      w->rec_count = counts + t;
+      const uint32_t sub = t % w->cfg.substeps;
+      enqueue_substep(w, dt_sub, w->old_dt, w->pending, sub == 0, sub + 1 == w->cfg.substeps);
+      w->pending = false;
+      if (w->any_dynamic) w->old_dt = dt_sub;
+      gather_state(w, sp + nb * (t + 1), nullptr, ss + nb * (t + 1), sv + nb * (t + 1));
+    }
+    w->rec_pairs = nullptr;
+    w->rec_count = nullptr;
+    w->rec_cap = 0;
+    e = cudaMemcpyAsync(hcounts.data(), counts, sizeof(uint32_t) * nsub, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (uint32_t t = 0; t < nsub && e == cudaSuccess; ++t)
+      if (hcounts[t] > cap) status = BLOBS_ERR_OVERFLOW;
+    // reverse substeps of the segment
+    for (int t = (int)nsub - 1; t >= 0 && status == BLOBS_OK; --t) {
+      AdjointSubstep a;
+      std::memset(&a, 0, sizeof(a));
+      a.p_t = sp + nb * t;
+      a.s_t = ss + nb * t;
+      a.v_t = w->has_springs ? sv + nb * t : nullptr;
+      a.p_t1 = sp + nb * (t + 1);
+      a.s_t1 = ss + nb * (t + 1);
+      a.pairs = pairs + (size_t)cap * t;
+      a.n_pairs = counts + t;
+      a.pair_cap = cap;
+      a.lp_in = adj[in][0];
+      a.lpo_in = adj[in][1];
+      a.ls_in = adj[in][2];
+      a.lv_in = adj[in][3];
+      a.lp_out = adj[in ^ 1][0];
+      a.lpo_out = adj[in ^ 1][1];
+      a.ls_out = adj[in ^ 1][2];
+      a.lv_out = adj[in ^ 1][3];
+      a.lpc = lpc;
+      a.la = la;
+      a.lv0 = lv0;
+      a.lk = lk;
+      a.dt = dt_sub;
+      a.ratio_first = dt_sub / r.old_dt0;
+      a.first_substep = (g == 0 && t == 0) ? 1u : 0u;
+      a.vreq_pending = (a.first_substep && r.pending0) ? 1u : 0u;
+      launch_adjoint_substep(w->dev, a, st);
+      in ^= 1;
+    }
+  }
+  w->timing = saved_timing;
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess && status == BLOBS_OK) {
+    if (dl_dvreq) e = cudaMemcpyAsync(dl_dvreq, lv0, slice, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && dl_dk && w->ns) e = cudaMemcpyAsync(dl_dk, lk, sizeof(float) * w->ns, cudaMemcpyDeviceToHost, st);
+  }
+  // errors flagged by the recomputed substeps stay sticky; then leave the
+  // world in the rollout's final state, counters as after the forward pass
+  if (e == cudaSuccess) {
+    const int rs = read_status(w);
+    if (rs && !status) status = rs;
+    const float2* fin = r.ckpt + 4 * nb * r.n_seg;
+    restore_state(w, fin, fin + nb, fin + 2 * nb, fin + 3 * nb);
+    w->old_dt = dt_sub;
+    w->pending = false;
+    e = cudaMemcpyAsync(w->dcounters, saved, sizeof(Counters), cudaMemcpyDeviceToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  if (status) return status;
+  return read_status(w);
 }
 
 int blobs_world_kernel_launches(blobs_world* w, uint64_t* count) {

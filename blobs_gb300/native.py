@@ -98,6 +98,8 @@ def lib() -> ctypes.CDLL:
         "blobs_world_set_stream": (i32, [_P, _P]),
         "blobs_world_write_bodies": (i32, [_P, _P, _P, _P, _P, _P]),
         "blobs_world_set_timing": (i32, [_P, i32]),
+        "blobs_world_rollout_record": (i32, [_P, f64, u32, u32]),
+        "blobs_world_backward": (i32, [_P, _P, _P, _P]),
         "blobs_world_emit_pairs": (i32, [_P, i32, _P, u64, ctypes.POINTER(u64)]),
         "blobs_world_grid": (i32, [_P, u32, ctypes.POINTER(f32), ctypes.POINTER(f32), _P, ctypes.POINTER(u32),
                                    ctypes.POINTER(u32)]),
@@ -309,6 +311,20 @@ class World:
         check(lib().blobs_world_grid(self._h, world, ctypes.byref(cs), ctypes.byref(inv), _ptr(org),
                                      ctypes.byref(lw), ctypes.byref(lh)), "grid")
         return cs.value, inv.value, org, lw.value, lh.value
+
+    def rollout_record(self, dt: float, n_steps: int, checkpoint_every: int = 16) -> None:
+        """Differentiable rollout: n_steps steps with checkpoints for backward()."""
+        check(lib().blobs_world_rollout_record(self._h, float(dt), int(n_steps), int(checkpoint_every)),
+              "rollout_record")
+
+    def backward(self, dl_dpos: np.ndarray, n_springs: int):
+        """dL/d(velocity requests) (n, 2) and dL/d(spring stiffness) (n_springs,)
+        of the last recorded rollout, given dL/d(final positions) (n, 2)."""
+        g = np.ascontiguousarray(dl_dpos, np.float32).reshape(self.n_bodies, 2)
+        gv = np.zeros((self.n_bodies, 2), np.float32)
+        gk = np.zeros(max(n_springs, 1), np.float32)
+        check(lib().blobs_world_backward(self._h, _ptr(g), _ptr(gv), _ptr(gk)), "backward")
+        return gv, gk[:n_springs]
 
     def kernel_launches(self) -> int:
         n = ctypes.c_uint64()

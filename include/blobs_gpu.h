@@ -230,6 +230,26 @@ int blobs_world_time(blobs_world* w, double* time, double* accumulator);
  * sorted by colour, then by arena index).  `order` holds n_joints entries. */
 int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours);
 
+/* ---- differentiable rollout (no counterpart in the reference) ---------------- */
+
+/* `n_steps` calls of step(delta) on a single-sphere world (every body one
+ * collider at offset zero, default groups, no sensor, no joints, no circle
+ * constraint; springs, walls, static bodies and batched worlds allowed),
+ * keeping the arena-order state every `checkpoint_every` steps for
+ * blobs_world_backward.  The velocity requests pending at the start (the
+ * RigidBodyBuilder::velocity_request of a fresh scene, rigid_body.rs:346-349)
+ * and the spring stiffnesses are the differentiable parameters. */
+int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, uint32_t checkpoint_every);
+/* Reverse pass of the last recorded rollout: given dL/d(final position)
+ * (2 n_bodies floats, host), writes dL/d(velocity request) (2 n_bodies,
+ * host, may be NULL) and dL/d(spring stiffness) (n_springs, host, may be
+ * NULL).  Each checkpoint segment is recomputed (bit-identical to the
+ * forward pass) with its contacts recorded, then reversed substep by
+ * substep.  Contacts resolved by the push-out branch (coincident centres,
+ * physics.rs:272-286) are not differentiated.  The world is left in the
+ * rollout's final state.  Synchronising. */
+int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk);
+
 /* ---- contact pairs without any allocation ------------------------------------ */
 
 /* No counterpart in the reference.  The contact pair set of

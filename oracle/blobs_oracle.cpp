@@ -276,6 +276,13 @@ class WorldBase {
   uint64_t last_substep_contacts = 0;
   double time = 0;
   std::vector<Event> events;
+  // Substep trace for checking derivatives along this world's own trajectory:
+  // the state at the start of every substep (position, position_old,
+  // collider snapshots, calculated_velocity) and the contacts it resolved.
+  bool tracing = false;
+  std::vector<double> trace_states;
+  std::vector<uint32_t> trace_pairs;    // (i, j | push-out << 31), collider ids, i > j
+  std::vector<uint64_t> trace_counts;   // contacts per substep
 };
 
 template <class T> class World : public WorldBase {
@@ -440,7 +447,8 @@ template <class T> class World : public WorldBase {
         if (distance < min_dist) {
           Body& ra = bodies[ca.parent];
           Body& rb = bodies[cb.parent];
-          if (distance < (T)1e-6f) {
+          const bool distance_pushed = distance < (T)1e-6f;
+          if (distance_pushed) {
             V2<T> push = {(T)0.01f, (T)0};
             ra.pos = ra.pos + push;
             rb.pos = rb.pos - push;
@@ -460,12 +468,17 @@ template <class T> class World : public WorldBase {
             rb.pos = rb.pos - (((T)1 - ratio) * delta) * n;
           }
           ++count;
+          if (tracing) {
+            trace_pairs.push_back(i);
+            trace_pairs.push_back(j | (distance_pushed ? 0x80000000u : 0u));
+          }
           if (record_events) events.push_back(Event{i, j, {(double)va.x, (double)va.y}, {(double)vb.x, (double)vb.y}});
         }
       }
     }
     contacts += count;
     last_substep_contacts = count;
+    if (tracing) trace_counts.push_back(count);
     return ORACLE_OK;
   }
 
@@ -561,6 +574,8 @@ template <class T> class World : public WorldBase {
   int integrate(uint32_t n_sub, T delta) {
     T step_delta = delta / (T)n_sub;
     for (uint32_t s = 0; s < n_sub; ++s) {
+      if (tracing) trace_state();
+      if (tracing && !collisions_enabled) trace_counts.push_back(0);
       apply_gravity();
       apply_springs();
       if (collisions_enabled) {
@@ -573,6 +588,14 @@ template <class T> class World : public WorldBase {
       apply_constraints();
     }
     return ORACLE_OK;
+  }
+
+  void trace_state() {
+    for (const Body& b : bodies) trace_states.push_back((double)b.pos.x), trace_states.push_back((double)b.pos.y);
+    for (const Body& b : bodies)
+      trace_states.push_back((double)b.pos_old.x), trace_states.push_back((double)b.pos_old.y);
+    for (const Collider& c : cols) trace_states.push_back((double)c.snap.x), trace_states.push_back((double)c.snap.y);
+    for (const Body& b : bodies) trace_states.push_back((double)b.vcalc.x), trace_states.push_back((double)b.vcalc.y);
   }
 
   // physics.rs:78-82
@@ -653,6 +676,32 @@ uint64_t oracle_world_events(void* w, uint32_t* a, uint32_t* b, double* va, doub
   return wb->events.size();
 }
 void oracle_world_clear_events(void* w) { static_cast<WorldBase*>(w)->events.clear(); }
+
+// Substep trace (test infrastructure for derivative checks): on != 0 clears
+// and starts it.  Each state is 2n position, 2n position_old, 2c snapshots,
+// 2n calculated_velocity, recorded at the start of every substep.
+void oracle_world_trace(void* w, int on) {
+  WorldBase* wb = static_cast<WorldBase*>(w);
+  wb->tracing = on != 0;
+  wb->trace_states.clear();
+  wb->trace_pairs.clear();
+  wb->trace_counts.clear();
+}
+uint64_t oracle_world_trace_states(void* w, double* out, uint64_t cap) {
+  const std::vector<double>& v = static_cast<WorldBase*>(w)->trace_states;
+  for (uint64_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
+  return v.size();
+}
+uint64_t oracle_world_trace_pairs(void* w, uint32_t* out, uint64_t cap) {
+  const std::vector<uint32_t>& v = static_cast<WorldBase*>(w)->trace_pairs;
+  for (uint64_t i = 0; i < v.size() && i < 2 * cap; ++i) out[i] = v[i];
+  return v.size() / 2;
+}
+uint64_t oracle_world_trace_counts(void* w, uint64_t* out, uint64_t cap) {
+  const std::vector<uint64_t>& v = static_cast<WorldBase*>(w)->trace_counts;
+  for (uint64_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
+  return v.size();
+}
 
 // update_mass_and_inertia over a whole scene (f32), rigid_body.rs:96-128.
 void oracle_mass_inertia_f32(const oracle_scene* s, float* mass, float* inertia) {

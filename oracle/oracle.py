@@ -66,6 +66,10 @@ def lib() -> ctypes.CDLL:
         "oracle_world_time": (f64, [_P]),
         "oracle_world_events": (u64, [_P, _P, _P, _P, _P, u64]),
         "oracle_world_clear_events": (None, [_P]),
+        "oracle_world_trace": (None, [_P, i32]),
+        "oracle_world_trace_states": (u64, [_P, _P, u64]),
+        "oracle_world_trace_pairs": (u64, [_P, _P, u64]),
+        "oracle_world_trace_counts": (u64, [_P, _P, u64]),
         "oracle_mass_inertia_f32": (None, [ctypes.POINTER(OracleScene), _P, _P]),
         "oracle_body_collider_transform": (None, [f32, f32, f32, f32, f32, _P]),
         "oracle_contact_pairs": (u64, [u32, _P, _P, _P, _P, _P, _P, _P, u64]),
@@ -234,6 +238,41 @@ class OracleWorld:
     @property
     def time(self) -> float:
         return float(lib().oracle_world_time(self._h))
+
+    def trace(self, on: bool = True) -> None:
+        """Start (and clear) or stop the substep trace."""
+        lib().oracle_world_trace(self._h, 1 if on else 0)
+
+    def traced(self):
+        """The substep trace: a list of per-substep dicts with the state at the
+        substep's start (pos, pos_old, snap, vel as float64 arrays) and the
+        contacts it resolved (hi, lo collider ids; pushed flags)."""
+        L = lib()
+        n, c = self.n_bodies, self.n_colliders
+        ns = int(L.oracle_world_trace_states(self._h, None, 0))
+        st = np.zeros(ns)
+        if ns:
+            L.oracle_world_trace_states(self._h, st.ctypes.data, ns)
+        npairs = int(L.oracle_world_trace_pairs(self._h, None, 0))
+        pr = np.zeros((npairs, 2), np.uint32)
+        if npairs:
+            L.oracle_world_trace_pairs(self._h, pr.ctypes.data, npairs)
+        nsub = int(L.oracle_world_trace_counts(self._h, None, 0))
+        counts = np.zeros(nsub, np.uint64)
+        if nsub:
+            L.oracle_world_trace_counts(self._h, counts.ctypes.data, nsub)
+        per = 6 * n + 2 * c
+        assert ns == per * nsub, (ns, per, nsub)
+        out, k = [], 0
+        for t in range(nsub):
+            x = st[per * t: per * (t + 1)]
+            q = pr[k: k + int(counts[t])]
+            k += int(counts[t])
+            out.append({"pos": x[:2 * n].reshape(n, 2), "pos_old": x[2 * n:4 * n].reshape(n, 2),
+                        "snap": x[4 * n:4 * n + 2 * c].reshape(c, 2), "vel": x[4 * n + 2 * c:].reshape(n, 2),
+                        "hi": q[:, 0].astype(np.int64), "lo": (q[:, 1] & 0x7FFFFFFF).astype(np.int64),
+                        "pushed": (q[:, 1] >> 31).astype(bool)})
+        return out
 
     def events(self):
         n = int(lib().oracle_world_events(self._h, None, None, None, None, 0))
