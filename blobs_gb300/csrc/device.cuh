@@ -112,6 +112,15 @@ struct WorldDev {
   uint32_t* ckey;            // per storage slot: cell the permute sorted the body into
   uint32_t* where;           // arena id -> storage slot
 
+  // collision event stream (NULL when off): one record per resolved pair,
+  // appended in any order and put in the reference's order on the host by
+  // (substep sequence, a, b)
+  uint4* ev_rec;             // (sequence, collider a, collider b, 0), a > b
+  float4* ev_vel;            // (impact_vel_a, impact_vel_b): calculated_velocity of the parents
+  uint32_t* ev_count;        // appended so far (may exceed ev_cap: overflow)
+  uint32_t* ev_seq;          // substep sequence number, advanced after each contact pass
+  uint32_t ev_cap;
+
   // counters, each spread over COUNTER_BINS bins that the host sums
   unsigned long long* contacts_total;
   unsigned long long* pushouts_total;
@@ -196,12 +205,24 @@ struct SingleArgs {
   const uint32_t* own_cell;  // cell of each storage slot in this substep's order
   float dt, ratio_first, ratio_rest;
   uint32_t contacts, pending, springs, rot_dynamic, do_keys, write_v, move_v;
+  uint32_t v_vel;            // V holds calculated_velocity (else the displacement of the last substep)
   // contact recording for the adjoint (NULL in ordinary steps): pairs
   // (hi, lo | pushed << 31) in arena ids
   uint2* rec_pairs;
   uint32_t* rec_count;
   uint32_t rec_cap;
 };
+
+// Append one collision event (physics.rs:304-311): the pair (a, b) with
+// a > b in collider order and the parents' calculated_velocity at the start
+// of the contact pass.
+__device__ __forceinline__ void record_event(const WorldDev& w, uint32_t a, uint32_t b, float2 va, float2 vb) {
+  const uint32_t k = atomicAdd(w.ev_count, 1u);
+  if (k < w.ev_cap) {
+    w.ev_rec[k] = make_uint4(*w.ev_seq, a, b, 0u);
+    w.ev_vel[k] = make_float4(va.x, va.y, vb.x, vb.y);
+  }
+}
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;

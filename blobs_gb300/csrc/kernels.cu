@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(256) k_contact_single(WorldDev w, const float2
       if (c > c2) {
         ++ncontacts;
         npush += po.pushed ? 1u : 0u;
+        if (w.ev_rec) record_event(w, c, c2, w.vel[c], w.vel[c2]);
       }
       if (po.pushed || nl >= CONTACT_LIST) {
         slow = true;
@@ -546,6 +547,7 @@ __global__ void __launch_bounds__(256) k_contact_general(WorldDev w, const float
         if (c > c2) {
           ++ncontacts;
           npush += po.pushed ? 1u : 0u;
+          if (w.ev_rec) record_event(w, c, c2, w.vel[b], w.vel[b2]);
         }
         if (po.pushed || nl >= CONTACT_LIST) {
           slow = true;
@@ -606,6 +608,23 @@ __global__ void __launch_bounds__(256) k_contact_general(WorldDev w, const float
     }
   }
   count_contacts(w, ncontacts, npush);
+}
+
+// Advances the collision-event substep sequence (after a contact pass).
+__global__ void k_ev_tick(WorldDev w) {
+  if (threadIdx.x == 0) *w.ev_seq += 1u;
+}
+
+void launch_ev_tick(const WorldDev& w, cudaStream_t st) { k_ev_tick<<<1, 32, 0, st>>>(w); }
+
+// Divides a V buffer of displacements by dt in place (storage order).
+__global__ void k_v_divide(float2* v, uint32_t n, float dt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = divs(v[i], dt);
+}
+
+void launch_v_divide(float2* v, uint32_t n, float dt, cudaStream_t st) {
+  if (n) k_v_divide<<<(n + 255u) / 256u, 256, 0, st>>>(v, n, dt);
 }
 
 // ---------------------------------------------------------------------------

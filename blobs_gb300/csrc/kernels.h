@@ -13,6 +13,8 @@ void launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, b
                      bool springs, bool pending, bool fuse, float dt, float old_dt, bool do_keys, bool rot_dynamic,
                      cudaStream_t st);
 void launch_joints(const WorldDev& w, float2* pos, uint32_t j0, uint32_t j1, float dt, cudaStream_t st);
+void launch_ev_tick(const WorldDev& w, cudaStream_t st);
+void launch_v_divide(float2* v, uint32_t n, float dt, cudaStream_t st);
 void launch_integrate(const WorldDev& w, const float2* pos_in, float2* pos_out, bool multiworld, bool single,
                       bool springs, bool pending, float dt, float old_dt, bool do_keys, bool rot_dynamic,
                       cudaStream_t st);

@@ -2,6 +2,7 @@
 // (include/blobs_physics.hpp) on top of the C ABI (include/blobs_gpu.h).
 #include "blobs_physics.hpp"
 
+#include <algorithm>
 #include <cstring>
 
 namespace blobs {
@@ -355,11 +356,51 @@ void Physics::pull() {
 
 void Physics::integrate(double delta) {
   push();
+  const uint32_t want = record_collision_events
+                            ? (uint32_t)std::min<uint64_t>(std::max<uint64_t>(65536, 64ull * col_slots_.size() *
+                                                                                        substeps / 8),
+                                                           0x7fffffffull)
+                            : 0u;
+  if (want > event_capacity_ || (!want && event_capacity_)) {
+    check(blobs_world_set_events(world_, want ? 1 : 0, want), "blobs_world_set_events");
+    event_capacity_ = want;
+  }
   check(blobs_world_step(world_, delta), "blobs_world_step");
   device_newer_ = true;
+  if (event_capacity_) drain_events();
   bool any_dynamic = false;
   rbd_set_.for_each([&](Index, const RigidBody& b) { any_dynamic = any_dynamic || !b.is_static(); });
   if (any_dynamic) old_dt = (float)delta / (float)substeps;  // physics.rs:339, last substep's dt
+}
+
+// Moves the device's events of the last step into events_ with handles.
+void Physics::drain_events() {
+  uint64_t n = 0, left = 0;
+  int st = blobs_world_drain_events(world_, nullptr, nullptr, nullptr, nullptr, 0, &n, &left);
+  if (st == BLOBS_ERR_OVERFLOW) {
+    // a step produced more events than the buffer holds: they are lost;
+    // enlarge the buffer for the next steps and report it
+    event_capacity_ = (uint32_t)std::min<uint64_t>(2 * left, 0x7fffffffull);
+    check(blobs_world_set_events(world_, 1, event_capacity_), "blobs_world_set_events");
+  }
+  check(st, "blobs_world_drain_events");
+  if (!left) return;
+  std::vector<uint32_t> a(left), b(left);
+  std::vector<float> va(2 * left), vb(2 * left);
+  check(blobs_world_drain_events(world_, a.data(), b.data(), va.data(), vb.data(), left, &n, nullptr),
+        "blobs_world_drain_events");
+  for (uint64_t k = 0; k < n; ++k) {
+    if (a[k] >= col_slots_.size() || b[k] >= col_slots_.size())
+      throw Error(BLOBS_ERR_INVALID_ARGUMENT, "collision event outside the collider arena");
+    events_.push_back(CollisionEvent{ColliderHandle{col_slots_[a[k]]}, ColliderHandle{col_slots_[b[k]]},
+                                     Vec2(va[2 * k], va[2 * k + 1]), Vec2(vb[2 * k], vb[2 * k + 1])});
+  }
+}
+
+std::vector<CollisionEvent> Physics::collision_events() {
+  std::vector<CollisionEvent> out;
+  out.swap(events_);
+  return out;
 }
 
 void Physics::step(double delta) {

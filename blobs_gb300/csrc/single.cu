@@ -159,6 +159,18 @@ __device__ __forceinline__ void record_pair(const SingleArgs& a, uint32_t hi, ui
   if (k < a.rec_cap) a.rec_pairs[k] = make_uint2(hi, lo | (pushed ? 0x80000000u : 0u));
 }
 
+// Collision event of the pair (c, lo), c > lo: velocities from the V buffer
+// (calculated_velocity while events are on) at both bodies' storage slots.
+__device__ __forceinline__ void single_event(const WorldDev& w, const SingleArgs& a, uint32_t c, uint32_t j,
+                                             uint32_t lo) {
+  const uint32_t jl = w.where[lo];
+  if (jl >= w.n_bodies) {
+    atomicOr(w.status, ST_BAD_INDEX);
+    return;
+  }
+  record_event(w, c, lo, a.v_in[j], a.v_in[jl]);
+}
+
 __device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush) {
   uint32_t t = ncontacts, p = npush;
 #pragma unroll
@@ -242,6 +254,7 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
       ++ncontacts;
       npush += sp.pushed ? 1u : 0u;
       if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
+      if (w.ev_rec) single_event(w, a, c, j, best);
     }
     last = best;
     first = false;
@@ -359,6 +372,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
             if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
+            if (w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
@@ -409,6 +423,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
             if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
+            if (w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
@@ -465,10 +480,10 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
         w.angvel[c] = avl;
         w.rot[c] = w.rot[c] + avl * dt;
       }
-      // calculated_velocity = disp / dt (physics.rs:357); without springs
-      // nothing reads it during the step, so the displacement is kept and
-      // divided when it is read
-      vel = a.springs ? divs(disp, dt) : disp;
+      // calculated_velocity = disp / dt (physics.rs:357); without springs or
+      // collision events nothing reads it during the step, so the
+      // displacement is kept and divided when it is read
+      vel = a.v_vel ? divs(disp, dt) : disp;
     }
     const float2 snap = v2(0.0f + p.x, 0.0f + p.y);  // rot(theta) * 0 + p
     for (uint32_t kk = 0; kk < w.n_circles; ++kk) {
@@ -484,7 +499,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
     }
     a.a_out[j] = make_float4(snap.x, snap.y, r, av.w);
     a.b_out[j] = make_float4(p.x, p.y, po.x, po.y);
-    if (a.springs || a.write_v) a.v_out[j] = vel;
+    if (a.v_vel || a.write_v) a.v_out[j] = vel;
     if (a.do_keys) {
       const uint32_t key = cell_key(wp, snap);
       w.key[j] = key;

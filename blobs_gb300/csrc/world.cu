@@ -8,7 +8,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <numeric>
 #include <vector>
 
 #include "blobs_gpu.h"
@@ -115,8 +117,8 @@ struct blobs_world {
   bool any_dynamic = false;
   bool sorted_storage = false;  // single-sphere path: body state in cell-sorted storage (single.cu)
   int single_mode = 1;          // 0: one uniform world, 1: one world, 2: batched (single.cu)
-  float v_div = 0.0f;           // sorted storage without springs: V[vbuf] holds the displacement of a substep of this dt
-  int vbuf = 0;                 // sorted storage without springs: the V buffer in use
+  float v_div = 0.0f;           // sorted storage, V untracked: V[vbuf] holds the displacement of a substep of this dt
+  int vbuf = 0;                 // sorted storage, V untracked: the V buffer in use
   bool pending = false;
   bool keys_valid = false;
   std::vector<uint32_t> colour_offsets;  // colour k = joints [colour_offsets[k], colour_offsets[k+1]) in processing order
@@ -147,6 +149,29 @@ struct blobs_world {
     bool pending0 = false;
     float2* ckpt = nullptr;  // (n_seg + 1) x 4 x n_bodies float2: p, po, s, v
   } rec;
+  // collision event stream (physics.rs:304-311), off unless enabled
+  struct HostEvent {
+    uint32_t a, b;
+    float va[2], vb[2];
+  };
+  bool events_on = false;
+  void* ev_mem = nullptr;
+  uint32_t ev_cap = 0;
+  uint4* ev_rec = nullptr;
+  float4* ev_vel = nullptr;
+  uint32_t* ev_count = nullptr;
+  uint32_t* ev_seq = nullptr;
+  std::deque<HostEvent> ev_host;       // drained from the device, in the reference's order
+  // sorted storage keeps calculated_velocity in V, double-buffered with the
+  // state, when something reads it during a step (springs, events)
+  bool v_tracks() const { return has_springs || events_on; }
+  void attach_events() {
+    dev.ev_rec = events_on ? ev_rec : nullptr;
+    dev.ev_vel = events_on ? ev_vel : nullptr;
+    dev.ev_count = events_on ? ev_count : nullptr;
+    dev.ev_seq = events_on ? ev_seq : nullptr;
+    dev.ev_cap = events_on ? ev_cap : 0u;
+  }
   bool capturing = false;
   TimingSet* recording = nullptr;      // set that enqueue_substep records into
   std::map<GraphKey, TimingSet> graph_timing;
@@ -173,6 +198,10 @@ struct blobs_world {
     drop_graphs();
     if (rec.ckpt) cudaFree(rec.ckpt);
     rec = Recording();
+    if (ev_mem) cudaFree(ev_mem);
+    ev_mem = nullptr;
+    events_on = false;
+    ev_host.clear();
     if (arena) cudaFree(arena);
     arena = nullptr;
     if (hcounters) cudaFreeHost(hcounters);
@@ -600,7 +629,8 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.springs = w->has_springs ? 1u : 0u;
     a.rot_dynamic = w->rot_dynamic ? 1u : 0u;
     a.write_v = last_in_step ? 1u : 0u;
-    a.move_v = w->has_springs ? 1u : 0u;
+    a.move_v = w->v_tracks() ? 1u : 0u;
+    a.v_vel = w->v_tracks() ? 1u : 0u;
     a.rec_pairs = w->rec_pairs;
     a.rec_count = w->rec_count;
     a.rec_cap = w->rec_cap;
@@ -642,15 +672,19 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     }
     a.a_in = d.sa[in];
     a.b_in = d.sb[in];
-    a.v_in = d.sv[w->has_springs ? in : w->vbuf];
+    a.v_in = d.sv[w->v_tracks() ? in : w->vbuf];
     a.a_out = d.sa[out];
     a.b_out = d.sb[out];
-    a.v_out = d.sv[w->has_springs ? out : w->vbuf];
+    a.v_out = d.sv[w->v_tracks() ? out : w->vbuf];
     mark_begin(w, coll ? PHASE_CONTACT : PHASE_INTEGRATE);
     launch_step_single(d, a, w->single_mode, st);
     mark_end(w);
+    if (coll && d.ev_rec) {
+      launch_ev_tick(d, st);
+      w->enqueued += 1;
+    }
     w->cur = (uint32_t)out;
-    if (!w->has_springs && last_in_step) w->v_div = dt;
+    if (!w->v_tracks() && last_in_step) w->v_div = dt;
     return;
   }
   if (coll && !w->keys_valid) {
@@ -670,12 +704,18 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     w->enqueued += 1;
   }
   if (coll) {
-    const bool fuse = !w->has_joints;
+    // events read the start-of-substep velocities, which the fused
+    // integration would overwrite in place
+    const bool fuse = !w->has_joints && !w->events_on;
     mark_begin(w, PHASE_CONTACT);
     launch_contacts(d, in, out, w->multiworld, w->single, w->has_springs, pending, fuse, dt, old_dt, true,
                     w->rot_dynamic, st);
     mark_end(w);
     w->enqueued += 1;
+    if (d.ev_rec) {
+      launch_ev_tick(d, st);
+      w->enqueued += 1;
+    }
     if (!fuse) {
       joints(out);
       mark_begin(w, PHASE_INTEGRATE);
@@ -761,7 +801,7 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
       w->launched_sets.push_back(ts);
   }
   w->cur = w->graph_cur_after[key];
-  if (w->sorted_storage && !w->has_springs) w->v_div = step_delta;
+  if (w->sorted_storage && !w->v_tracks()) w->v_div = step_delta;
   w->keys_valid = coll;
   return BLOBS_OK;
 }
@@ -801,14 +841,14 @@ int run_steps(blobs_world* w, double delta, uint32_t n_steps) {
 // n-body float2 slices (v only holds velocities in worlds with springs).
 void gather_state(blobs_world* w, float2* p, float2* po, float2* sn, float2* v) {
   const int c = (int)w->cur;
-  launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf], p, po,
-                       w->has_springs ? v : nullptr, sn, 0.0f, w->st());
+  launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->v_tracks() ? c : w->vbuf], p, po,
+                       w->v_tracks() ? v : nullptr, sn, 0.0f, w->st());
 }
 
 void restore_state(blobs_world* w, const float2* p, const float2* po, const float2* sn, const float2* v) {
   const int c = (int)w->cur;
-  launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf], p, po,
-                      w->has_springs ? v : nullptr, sn, w->st());
+  launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->v_tracks() ? c : w->vbuf], p, po,
+                      w->v_tracks() ? v : nullptr, sn, w->st());
   // the snapshots changed: the next substep recounts the cells from zero
   cudaMemsetAsync(w->dev.cell_count, 0, sizeof(uint32_t) * (size_t)w->dev.n_cells, w->st());
   w->keys_valid = false;
@@ -1050,6 +1090,12 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
     return blobs_map_cuda(e);
   }
   w->dev = d;
+  w->attach_events();
+  if (w->events_on) {
+    // a reloaded world starts a new event stream
+    w->ev_host.clear();
+    cudaMemsetAsync(w->ev_count, 0, 2 * sizeof(uint32_t), s);
+  }
   w->nb = nb;
   w->nc = nc;
   w->ns = ns;
@@ -1124,7 +1170,7 @@ int blobs_world_read_bodies(blobs_world* w, float* pos, float* pos_old, float* v
   if (w->sorted_storage) {
     // storage order -> arena order into the staging arrays, then copy out
     const int c = (int)w->cur;
-    launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf],
+    launch_gather_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->v_tracks() ? c : w->vbuf],
                          pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr,
                          nullptr, w->v_div, s);
     e = cudaGetLastError();
@@ -1217,7 +1263,7 @@ int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_
   if (e == cudaSuccess && w->sorted_storage && n) {
     // arena order staging -> storage order
     const int c = (int)w->cur;
-    launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->has_springs ? c : w->vbuf],
+    launch_write_single(w->dev, w->dev.sa[c], w->dev.sb[c], w->dev.sv[w->v_tracks() ? c : w->vbuf],
                         pos ? w->pos[0] : nullptr, pos_old ? w->dev.pos_old : nullptr, vel ? w->dev.vel : nullptr,
                         nullptr, s);
     if (vel) w->v_div = 0.0f;  // every V entry is now a velocity
@@ -1254,7 +1300,7 @@ int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, u
     a.a_in = w->dev.sa[c];
     a.b_in = w->dev.sb[c];
     // V moves with the records; without springs it lives in its own buffer
-    const int vi = w->has_springs ? c : w->vbuf;
+    const int vi = w->v_tracks() ? c : w->vbuf;
     a.v_in = w->dev.sv[vi];
     a.a_out = w->dev.sa[c ^ 1];
     a.b_out = w->dev.sb[c ^ 1];
@@ -1262,7 +1308,7 @@ int blobs_world_emit_pairs(blobs_world* w, int contacts_only, uint32_t* pairs, u
     a.move_v = 1u;
     launch_permute(w->dev, a, s);
     w->cur ^= 1u;  // the permuted storage becomes current
-    if (!w->has_springs) w->vbuf ^= 1;
+    if (!w->v_tracks()) w->vbuf ^= 1;
     dv.sorted = w->dev.sa[w->cur];
   } else {
     if (!w->keys_valid) launch_keys(w->dev, w->multiworld, s);
@@ -1326,7 +1372,7 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
   const size_t nb = w->nb;
   cudaError_t e = cudaMalloc(&r.ckpt, sizeof(float2) * 4 * nb * (n_seg + 1));
   if (e != cudaSuccess) return blobs_map_cuda(e);
-  if (w->has_springs) e = cudaMemsetAsync(r.ckpt, 0, sizeof(float2) * 4 * nb * (n_seg + 1), w->st());
+  if (e == cudaSuccess) e = cudaMemsetAsync(r.ckpt, 0, sizeof(float2) * 4 * nb * (n_seg + 1), w->st());
   r.delta = delta;
   r.n_steps = n_steps;
   r.every = checkpoint_every;
@@ -1407,6 +1453,8 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   const float dt_sub = (float)r.delta / (float)w->cfg.substeps;
   const bool saved_timing = w->timing;
   w->timing = false;
+  // the recomputed substeps are not new collisions: no events
+  w->dev.ev_rec = nullptr;
   int status = BLOBS_OK;
   std::vector<uint32_t> hcounts(S);
   for (int g = (int)r.n_seg - 1; g >= 0 && e == cudaSuccess && status == BLOBS_OK; --g) {
@@ -1471,6 +1519,7 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
     }
   }
   w->timing = saved_timing;
+  w->attach_events();
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e == cudaSuccess && status == BLOBS_OK) {
     if (dl_dvreq) e = cudaMemcpyAsync(dl_dvreq, lv0, slice, cudaMemcpyDeviceToHost, st);
@@ -1491,6 +1540,125 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   cudaFree(buf);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   if (status) return status;
+  return read_status(w);
+}
+
+int blobs_world_set_events(blobs_world* w, int enabled, uint32_t capacity) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (enabled && (capacity == 0 || capacity > 0x7fffffffu)) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  cudaStream_t st = w->st();
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  const bool was_on = w->events_on;
+  w->drop_graphs();  // the event pointers and the fusion choice are baked into graphs
+  if (w->ev_mem) cudaFree(w->ev_mem);
+  w->ev_mem = nullptr;
+  w->ev_host.clear();
+  w->events_on = false;
+  if (enabled) {
+    Carver sizer;
+    auto lay = [&](Carver& cv) {
+      w->ev_rec = cv.take<uint4>(capacity);
+      w->ev_vel = cv.take<float4>(capacity);
+      w->ev_count = cv.take<uint32_t>(2);  // count, then the substep sequence
+    };
+    lay(sizer);
+    e = cudaMalloc(&w->ev_mem, sizer.off + 256);
+    if (e != cudaSuccess) {
+      w->ev_mem = nullptr;
+      w->attach_events();
+      return blobs_map_cuda(e);
+    }
+    Carver cv;
+    cv.base = static_cast<char*>(w->ev_mem);
+    lay(cv);
+    w->ev_seq = w->ev_count + 1;
+    w->ev_cap = capacity;
+    e = cudaMemsetAsync(w->ev_count, 0, 2 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return blobs_map_cuda(e);
+    w->events_on = true;
+  }
+  if (w->loaded && w->sorted_storage && !w->has_springs && w->events_on != was_on) {
+    const int c = (int)w->cur;
+    if (w->events_on) {
+      // V becomes calculated_velocity, double-buffered with the state
+      if (w->vbuf != c) e = cudaMemcpyAsync(w->dev.sv[c], w->dev.sv[w->vbuf], sizeof(float2) * w->nb,
+                                            cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess && w->v_div != 0.0f) launch_v_divide(w->dev.sv[c], w->nb, w->v_div, st);
+    }
+    w->vbuf = c;
+    w->v_div = 0.0f;
+  }
+  w->attach_events();
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return blobs_map_cuda(e);
+}
+
+int blobs_world_drain_events(blobs_world* w, uint32_t* col_a, uint32_t* col_b, float* impact_vel_a,
+                             float* impact_vel_b, uint64_t cap, uint64_t* n_written, uint64_t* n_left) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!n_written || (cap && (!col_a || !col_b))) return BLOBS_ERR_INVALID_ARGUMENT;
+  *n_written = 0;
+  if (n_left) *n_left = 0;
+  if (!w->events_on) return BLOBS_ERR_STATE;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  cudaStream_t st = w->st();
+  uint32_t head[2] = {0, 0};
+  e = cudaMemcpyAsync(head, w->ev_count, sizeof(head), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  const uint32_t n = head[0];
+  if (n > w->ev_cap) {
+    // the appended subset is not a prefix of the reference order: drop it
+    e = cudaMemsetAsync(w->ev_count, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (n_left) *n_left = n;
+    return e == cudaSuccess ? BLOBS_ERR_OVERFLOW : blobs_map_cuda(e);
+  }
+  if (n) {
+    std::vector<uint4> rec(n);
+    std::vector<float4> vel(n);
+    e = cudaMemcpyAsync(rec.data(), w->ev_rec, sizeof(uint4) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(vel.data(), w->ev_vel, sizeof(float4) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->ev_count, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return blobs_map_cuda(e);
+    // the reference's order: substep by substep, outer collider ascending,
+    // inner collider ascending (physics.rs:247-248)
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+      const uint4 &p = rec[x], &q = rec[y];
+      if (p.x != q.x) return (int32_t)(p.x - q.x) < 0;  // sequence, modulo 2^32
+      if (p.y != q.y) return p.y < q.y;
+      return p.z < q.z;
+    });
+    for (uint32_t k : order) {
+      blobs_world::HostEvent ev;
+      ev.a = rec[k].y;
+      ev.b = rec[k].z;
+      ev.va[0] = vel[k].x;
+      ev.va[1] = vel[k].y;
+      ev.vb[0] = vel[k].z;
+      ev.vb[1] = vel[k].w;
+      w->ev_host.push_back(ev);
+    }
+  }
+  uint64_t k = 0;
+  while (k < cap && !w->ev_host.empty()) {
+    const blobs_world::HostEvent& ev = w->ev_host.front();
+    col_a[k] = ev.a;
+    col_b[k] = ev.b;
+    if (impact_vel_a) impact_vel_a[2 * k] = ev.va[0], impact_vel_a[2 * k + 1] = ev.va[1];
+    if (impact_vel_b) impact_vel_b[2 * k] = ev.vb[0], impact_vel_b[2 * k + 1] = ev.vb[1];
+    w->ev_host.pop_front();
+    ++k;
+  }
+  *n_written = k;
+  if (n_left) *n_left = w->ev_host.size();
   return read_status(w);
 }
 

@@ -105,6 +105,8 @@ def lib() -> ctypes.CDLL:
                                    ctypes.POINTER(u32)]),
         "blobs_world_kernel_launches": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_phase_times": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(u64), u32]),
+        "blobs_world_set_events": (i32, [_P, i32, u32]),
+        "blobs_world_drain_events": (i32, [_P, _P, _P, _P, _P, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -325,6 +327,27 @@ class World:
         gk = np.zeros(max(n_springs, 1), np.float32)
         check(lib().blobs_world_backward(self._h, _ptr(g), _ptr(gv), _ptr(gk)), "backward")
         return gv, gk[:n_springs]
+
+    def set_events(self, enabled: bool = True, capacity: int = 1 << 20) -> None:
+        """Record CollisionEvents (physics.rs:304-311) into a device buffer of `capacity`."""
+        check(lib().blobs_world_set_events(self._h, 1 if enabled else 0, int(capacity) if enabled else 0),
+              "set_events")
+
+    def drain_events(self, cap: Optional[int] = None):
+        """collision_recv.try_iter(): (a, b, impact_vel_a, impact_vel_b) of the
+        events since the last drain, in the reference's order."""
+        n, left = ctypes.c_uint64(), ctypes.c_uint64()
+        if cap is None:
+            st = lib().blobs_world_drain_events(self._h, None, None, None, None, 0, ctypes.byref(n),
+                                                ctypes.byref(left))
+            check(st, "drain_events")
+            cap = int(left.value)
+        a, b = np.zeros(max(cap, 1), np.uint32), np.zeros(max(cap, 1), np.uint32)
+        va, vb = np.zeros((max(cap, 1), 2), np.float32), np.zeros((max(cap, 1), 2), np.float32)
+        check(lib().blobs_world_drain_events(self._h, _ptr(a), _ptr(b), _ptr(va), _ptr(vb), cap, ctypes.byref(n),
+                                             ctypes.byref(left)), "drain_events")
+        k = int(n.value)
+        return a[:k], b[:k], va[:k], vb[:k]
 
     def kernel_launches(self) -> int:
         n = ctypes.c_uint64()

@@ -247,8 +247,39 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
  * forward pass) with its contacts recorded, then reversed substep by
  * substep.  Contacts resolved by the push-out branch (coincident centres,
  * physics.rs:272-286) are not differentiated.  The world is left in the
- * rollout's final state.  Synchronising. */
+ * rollout's final state.  Allocates its scratch per call: 24 B per body per
+ * recorded substep state plus 8 B x (4 n_bodies + 1024) per substep of one
+ * checkpoint segment.  The derivative of long contact-rich rollouts can
+ * exceed the f32 range; such gradients come back as +-inf or NaN with
+ * BLOBS_OK.  Synchronising. */
 int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk);
+
+/* ---- collision events -------------------------------------------------------- */
+
+/* Replaces the CollisionEvent channel (lib.rs:146-153): Physics::new's
+ * std::sync::mpsc channel (physics.rs:37) and the send of one event per
+ * resolved pair in brute_force_collisions (physics.rs:304-311).  Off by
+ * default (events cost device bandwidth); enabled, every contact pass
+ * appends (collider a, collider b, impact_vel_a, impact_vel_b) for each
+ * pair in contact -- a > b in arena order, sensors included, the impact
+ * velocities being the parents' calculated_velocity at the start of the
+ * pass -- into a device buffer of `capacity` events.  Enabling or disabling
+ * discards undrained events; a reload (blobs_world_load) starts a new
+ * stream.  Batched worlds share one stream with scene-global collider
+ * indices.  Not synchronising. */
+int blobs_world_set_events(blobs_world* w, int enabled, uint32_t capacity);
+/* collision_recv.try_iter(): moves the events produced since the last drain
+ * to the host in the reference's order (substep by substep; outer collider
+ * ascending, then inner collider ascending) and writes up to `cap` of them
+ * (impact velocities as 2 floats each; either velocity array may be NULL).
+ * *n_written = events written, *n_left (may be NULL) = events kept for the
+ * next call.  If the device buffer overflowed since the last drain the
+ * whole batch is dropped (it is not a prefix of the reference's order):
+ * returns BLOBS_ERR_OVERFLOW with *n_left = events produced, so the caller
+ * can enlarge the capacity.  BLOBS_ERR_STATE when events are off.
+ * Synchronising. */
+int blobs_world_drain_events(blobs_world* w, uint32_t* col_a, uint32_t* col_b, float* impact_vel_a,
+                             float* impact_vel_b, uint64_t cap, uint64_t* n_written, uint64_t* n_left);
 
 /* ---- contact pairs without any allocation ------------------------------------ */
 

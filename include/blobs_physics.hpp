@@ -57,6 +57,14 @@ struct ColliderHandle { Index idx; bool operator==(const ColliderHandle& o) cons
 struct JointHandle { Index idx; bool operator==(const JointHandle& o) const { return idx == o.idx; } };
 struct SpringHandle { Index idx; bool operator==(const SpringHandle& o) const { return idx == o.idx; } };
 
+/// CollisionEvent (lib.rs:146-153): one per pair in contact per substep.
+struct CollisionEvent {
+  ColliderHandle col_handle_a;
+  ColliderHandle col_handle_b;
+  Vec2 impact_vel_a;
+  Vec2 impact_vel_b;
+};
+
 /// Generational arena with thunderdome's observable behaviour.
 template <class T> class Arena {
  public:
@@ -315,6 +323,13 @@ class Physics {
   /// reference's "collisions" perf counter).
   uint64_t contact_count();
 
+  /// collision_recv.try_iter() (physics.rs:37, :304-311): the collision
+  /// events of the steps since the last call, in the reference's order.
+  std::vector<CollisionEvent> collision_events();
+  /// The reference's channel always receives; turning this off skips the
+  /// device-side recording (and its bandwidth).
+  bool record_collision_events = true;
+
   const Arena<RigidBody>& rbd_set() { pull(); return rbd_set_; }
   const Arena<Collider>& col_set() { pull(); return col_set_; }
   const Arena<FixedJoint>& joints() const { return joints_; }
@@ -330,8 +345,11 @@ class Physics {
   Arena<Spring> springs_;
   blobs_world* world_ = nullptr;
   int device_ = 0;
+  void drain_events();
   bool host_dirty_ = true;     // arenas changed since the last upload
   bool device_newer_ = false;  // the device stepped since the last pull
+  uint32_t event_capacity_ = 0;  // device event buffer (0: recording off)
+  std::vector<CollisionEvent> events_;
   std::vector<Index> body_slots_, col_slots_;  // dense device index -> arena index
 };
 

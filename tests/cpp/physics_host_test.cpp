@@ -91,7 +91,8 @@ static int cpu_tests() {
 }
 
 // IN: u32 n, f32 gravity[2], f32 box[4], then per body: pos[2], vel[2], radius, u8 type
-// OUT: per body pos[2], pos_old[2], vel[2]; then u64 contacts
+// OUT: per body pos[2], pos_old[2], vel[2]; then u64 contacts; then u64
+// events and per event u32 collider slot a, b, f32 impact_vel_a[2], _b[2]
 static int scene_test(const char* in, const char* out, int steps, double dt) {
   FILE* f = std::fopen(in, "rb");
   if (!f) return 2;
@@ -115,7 +116,12 @@ static int scene_test(const char* in, const char* out, int steps, double dt) {
     hs.push_back(h);
   }
   std::fclose(f);
-  for (int s = 0; s < steps; ++s) p.step(dt);
+  std::vector<CollisionEvent> events;
+  for (int s = 0; s < steps; ++s) {
+    p.step(dt);
+    std::vector<CollisionEvent> e = p.collision_events();
+    events.insert(events.end(), e.begin(), e.end());
+  }
   FILE* o = std::fopen(out, "wb");
   for (RigidBodyHandle h : hs) {
     const RigidBody* b = p.get_rbd(h);
@@ -125,6 +131,14 @@ static int scene_test(const char* in, const char* out, int steps, double dt) {
   }
   uint64_t contacts = p.contact_count();
   std::fwrite(&contacts, 8, 1, o);
+  const uint64_t n_events = events.size();
+  std::fwrite(&n_events, 8, 1, o);
+  for (const CollisionEvent& e : events) {
+    const uint32_t ab[2] = {e.col_handle_a.idx.slot, e.col_handle_b.idx.slot};
+    const float v[4] = {e.impact_vel_a.x, e.impact_vel_a.y, e.impact_vel_b.x, e.impact_vel_b.y};
+    std::fwrite(ab, 4, 2, o);
+    std::fwrite(v, 4, 4, o);
+  }
   std::fclose(o);
   return 0;
 }

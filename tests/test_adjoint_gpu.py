@@ -269,3 +269,46 @@ def test_recorded_rollout_equals_plain_steps(n_worlds):
         assert np.array_equal(a[k], b[k])
         assert np.array_equal(a2[k], b2[k])
     assert ca == cb
+
+
+def test_autograd_function_wrapper():
+    """torch.autograd.Function around rollout_record / backward (test harness
+    only): the gradients torch accumulates are the direct backward's."""
+    torch = pytest.importorskip("torch")
+    scene, marked, targets = make_scene(seed=31, n_worlds=2)
+    steps, every = 4, 2
+
+    class Rollout(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, v0, k):
+            s = scene.copy()
+            s.vreq = v0.detach().numpy().astype(np.float32)
+            s.spr_k = k.detach().numpy().astype(np.float32)
+            w = native.World(s)
+            w.rollout_record(s.dt, steps, every)
+            ctx.world = w
+            return torch.from_numpy(w.read_bodies()["pos"].astype(np.float64))
+
+        @staticmethod
+        def backward(ctx, grad_pos):
+            w = ctx.world
+            gv, gk = w.backward(grad_pos.numpy().astype(np.float32), scene.n_springs)
+            w.close()
+            return torch.from_numpy(gv.astype(np.float64)), torch.from_numpy(gk.astype(np.float64))
+
+    v0 = torch.tensor(scene.vreq.astype(np.float64), requires_grad=True)
+    k = torch.tensor(scene.spr_k.astype(np.float64), requires_grad=True)
+    pos = Rollout.apply(v0, k)
+    M = sum(len(m) for m in marked)
+    loss = 0.0
+    for w, (m, t) in enumerate(zip(marked, targets)):
+        b0 = int(scene.world_body_offsets[w])
+        d = pos[torch.from_numpy(b0 + m)] - torch.from_numpy(t)
+        loss = loss + (d * d).sum() / M
+    loss.backward()
+    final, g, after, gv, gk = gpu_gradients(scene, marked, targets, steps, every)
+    assert np.array_equal(pos.detach().numpy(), final)
+    # the adjoint sums contact and spring terms with float atomics: equal up
+    # to the order of those additions
+    for got, want in ((v0.grad.numpy(), gv), (k.grad.numpy(), gk)):
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()

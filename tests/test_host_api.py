@@ -49,11 +49,23 @@ def test_host_mirror_steps_bit_exact(host_test_bin, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     raw = open(outp, "rb").read()
     got = np.frombuffer(raw[:24 * s.n_bodies], np.float32).reshape(-1, 6)
-    contacts = int(np.frombuffer(raw[24 * s.n_bodies:], np.uint64)[0])
-    w = oracle.OracleWorld(s, 32)
+    off = 24 * s.n_bodies
+    contacts, n_events = (int(x) for x in np.frombuffer(raw[off:off + 16], np.uint64))
+    ev = raw[off + 16:]
+    assert len(ev) == 24 * n_events
+    ev_ids = np.frombuffer(ev, np.uint32).reshape(-1, 6)[:, :2]
+    ev_vel = np.frombuffer(ev, np.float32).reshape(-1, 6)[:, 2:]
+    w = oracle.OracleWorld(s, 32, record_events=True)
     assert w.step(s.dt, steps) == 0
     want = w.bodies()
     np.testing.assert_array_equal(got[:, 0:2].astype(np.float64), want["pos"])
     np.testing.assert_array_equal(got[:, 2:4].astype(np.float64), want["pos_old"])
     np.testing.assert_array_equal(got[:, 4:6].astype(np.float64), want["vel"])
     assert contacts == w.contacts
+    # Physics::collision_events() (the collision_recv channel) in the reference's order
+    a, b, va, vb = w.events()
+    assert n_events == len(a) > 0
+    np.testing.assert_array_equal(ev_ids[:, 0], a)
+    np.testing.assert_array_equal(ev_ids[:, 1], b)
+    np.testing.assert_array_equal(ev_vel[:, 0:2].astype(np.float64), va)
+    np.testing.assert_array_equal(ev_vel[:, 2:4].astype(np.float64), vb)
