@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libblobs_gb300.so")
-SOURCES = ["kernels.cu", "single.cu", "adjoint.cu", "world.cu", "noalloc.cu", "physics.cpp"]
+SOURCES = ["kernels.cu", "single.cu", "adjoint.cu", "world.cu", "noalloc.cu", "spatial.cu", "physics.cpp"]
 HEADERS = ["device.cuh", "kernels.h", "world.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",

@@ -106,6 +106,10 @@ def lib() -> ctypes.CDLL:
         "blobs_world_kernel_launches": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_phase_times": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(u64), u32]),
         "blobs_world_set_events": (i32, [_P, i32, u32]),
+        "blobs_spatial_hash_create": (i32, [f32, i32, pp]),
+        "blobs_spatial_hash_destroy": (i32, [_P]),
+        "blobs_spatial_hash_set_points": (i32, [_P, u64, _P, _P, _P]),
+        "blobs_spatial_hash_query": (i32, [_P, u64, _P, _P, _P, _P, u64, ctypes.POINTER(u64)]),
         "blobs_world_drain_events": (i32, [_P, _P, _P, _P, _P, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
     }
     for name, (res, args) in sigs.items():
@@ -398,3 +402,56 @@ class World:
         nc = ctypes.c_uint32()
         check(lib().blobs_world_joint_order(self._h, _ptr(order), ctypes.byref(nc)), "joint_order")
         return order[:self.n_joints], int(nc.value)
+
+
+class SpatialHash:
+    """SpatialHash (spatial.rs) on the device: set_points replaces the point
+    set; query runs SpatialHash::query for many query points."""
+
+    def __init__(self, cell_size: float, device: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().blobs_spatial_hash_create(float(cell_size), int(device), ctypes.byref(h)),
+              "blobs_spatial_hash_create")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().blobs_spatial_hash_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_points(self, ids, xy, radius) -> None:
+        ids = np.ascontiguousarray(ids, np.uint64)
+        xy = np.ascontiguousarray(xy, np.float32).reshape(-1, 2)
+        radius = np.ascontiguousarray(radius, np.float32)
+        check(lib().blobs_spatial_hash_set_points(self._h, len(ids), _ptr(ids), _ptr(xy), _ptr(radius)),
+              "blobs_spatial_hash_set_points")
+
+    def query(self, qxy, qradius, cap: Optional[int] = None):
+        """(offsets (nq + 1,), ids) with each query's ids ascending."""
+        qxy = np.ascontiguousarray(qxy, np.float32).reshape(-1, 2)
+        qradius = np.ascontiguousarray(qradius, np.float32)
+        nq = len(qradius)
+        offsets = np.zeros(nq + 1, np.uint64)
+        total = ctypes.c_uint64()
+        if cap is None:
+            st = lib().blobs_spatial_hash_query(self._h, nq, _ptr(qxy), _ptr(qradius), _ptr(offsets), None, 0,
+                                                ctypes.byref(total))
+            if st not in (OK, ERR_OVERFLOW):
+                check(st, "blobs_spatial_hash_query")
+            cap = int(total.value)
+        ids = np.zeros(max(cap, 1), np.uint64)
+        check(lib().blobs_spatial_hash_query(self._h, nq, _ptr(qxy), _ptr(qradius), _ptr(offsets), _ptr(ids), cap,
+                                             ctypes.byref(total)), "blobs_spatial_hash_query")
+        return offsets, ids[:int(total.value)]

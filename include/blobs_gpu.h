@@ -281,6 +281,32 @@ int blobs_world_set_events(blobs_world* w, int enabled, uint32_t capacity);
 int blobs_world_drain_events(blobs_world* w, uint32_t* col_a, uint32_t* col_b, float* impact_vel_a,
                              float* impact_vel_b, uint64_t cap, uint64_t* n_written, uint64_t* n_left);
 
+/* ---- spatial hash queries ---------------------------------------------------- */
+
+/* SpatialHash (blobs/src/spatial.rs:31-195) on a device: a set of points
+ * (id, position, radius) bucketed by the reference's integer cell
+ * ((x / cell_size).floor() as i32, same for y; spatial.rs:57-62), and
+ * SpatialHash::query (spatial.rs:155-195) for many query points at once. */
+typedef struct blobs_spatial_hash blobs_spatial_hash;
+/* SpatialHash::new (spatial.rs:45-56). */
+int blobs_spatial_hash_create(float cell_size, int32_t device, blobs_spatial_hash** out);
+int blobs_spatial_hash_destroy(blobs_spatial_hash* h);
+/* Replaces the point set, as insert_with_id (spatial.rs:71-84) of every point
+ * into an empty hash: n points, ids unique (duplicate ids give unspecified
+ * results), xy 2n floats, radius n floats; host memory, copied.
+ * Synchronising. */
+int blobs_spatial_hash_set_points(blobs_spatial_hash* h, uint64_t n, const uint64_t* ids, const float* xy,
+                                  const float* radius);
+/* SpatialHash::query for nq query points (qxy 2nq floats, qradius nq):
+ * every point of the 3x3 cells around the query point's cell with
+ * |p - q|^2 <= (query_radius + radius)^2.  offsets (nq + 1, host) delimit
+ * each query's ids in `ids` (host, ascending per query; the reference's order
+ * is its HashMap's, unspecified).  *total = number of results; if it exceeds
+ * `cap` nothing is written to `ids` and BLOBS_ERR_OVERFLOW is returned with
+ * the offsets filled (call again with cap >= *total).  Synchronising. */
+int blobs_spatial_hash_query(blobs_spatial_hash* h, uint64_t nq, const float* qxy, const float* qradius,
+                             uint64_t* offsets, uint64_t* ids, uint64_t cap, uint64_t* total);
+
 /* ---- contact pairs without any allocation ------------------------------------ */
 
 /* No counterpart in the reference.  The contact pair set of
