@@ -138,6 +138,23 @@ def cpu_baseline(sizes=(4096, 8192, 16384, 32768), target_n=1_000_000, seed=2, s
     }
 
 
+def max_over_ranks(value, dist, device):
+    """The largest `value` over all ranks (the job's time is its slowest
+    rank's); `dist` is torch.distributed or None for one process."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(bodies_per_rank, steps, world_size, total_ms):
+    """Whole-job sphere-steps/s: every rank steps its own world of
+    `bodies_per_rank` bodies `steps` times; the job takes `total_ms`."""
+    return world_size * bodies_per_rank * steps / (total_ms / 1e3)
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm's CPU implementation (the
     oracle port; the Rust crate cannot be built here), rank 0 only."""
@@ -338,12 +355,8 @@ def run_ours(args):
     clk = clocks.stop()
     launches = world.kernel_launches() - k0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = world_size * scene.n_bodies * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(step_ms), dist, dev)
+    value = job_throughput(scene.n_bodies, args.steps, world_size, total_ms)
 
     # -- per-phase kernel time (events captured into the step graph) ---------
     world.set_timing(True)
@@ -378,10 +391,7 @@ def run_ours(args):
         world.step(dt)
         world.read_bodies_into(h_pos, h_old, h_vel)   # synchronising
         e2e_s.append(time.perf_counter() - t0)
-    e2e_t = torch.tensor([sum(e2e_s)], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = world_size * n * args.steps / float(e2e_t.item())
+    e2e_value = job_throughput(n, args.steps, world_size, 1e3 * max_over_ranks(sum(e2e_s), dist, dev))
     contacts_total, contacts_last = world.contact_count()
     world.sync()
 
