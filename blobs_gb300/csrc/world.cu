@@ -136,6 +136,7 @@ struct blobs_world {
   std::map<GraphKey, uint32_t> graph_cur_after;  // storage buffer holding the state after the graph
   cudaStream_t user_stream = nullptr;  // caller's stream (NULL: the world's own)
   bool timing = false;
+  float cell_scale = 1.0f;             // cell edge = scale x the smallest exact edge (autotuned)
   // contact recording of the eager path (adjoint recomputation)
   uint2* rec_pairs = nullptr;
   uint32_t* rec_count = nullptr;
@@ -249,7 +250,7 @@ bool check_offsets(const uint32_t* off, uint32_t nw, uint32_t total) {
   return true;
 }
 
-int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h) {
+int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scene& s, HostScene& h) {
   const uint32_t nw = s.n_worlds ? s.n_worlds : 1;
   const uint32_t nb = s.n_bodies, nc = s.n_colliders, ns = s.n_springs, nj = s.n_joints;
   if (nb && (!s.pos || !s.mass || !s.inertia)) return BLOBS_ERR_INVALID_ARGUMENT;
@@ -466,7 +467,9 @@ int build_host_scene(const blobs_config& cfg, const blobs_scene& s, HostScene& h
     // The 3x3 search is exact when cs >= 2 * rmax; the 1/64 margin absorbs
     // the rounding of v / cs for coordinates up to ~1e5 cells.
     const float safe = rmax > 0.0f ? 2.0f * rmax * (1.0f + 1.0f / 64.0f) : 1.0f;
-    const float cs = cfg.cell_size > safe ? cfg.cell_size : safe;
+    // cell_scale >= 1 (the autotuner's choice) only enlarges cells
+    const float tuned = safe * std::max(cell_scale, 1.0f);
+    const float cs = cfg.cell_size > tuned ? cfg.cell_size : tuned;
     if (s.world_box) {  // bodies stay inside the walls: grid the whole box
       lo_x = std::min(lo_x, s.world_box[4 * w + 0]);
       lo_y = std::min(lo_y, s.world_box[4 * w + 1]);
@@ -962,7 +965,7 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   cudaError_t e = cudaSetDevice(w->cfg.device);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   HostScene h;
-  int st = build_host_scene(w->cfg, *scene, h);
+  int st = build_host_scene(w->cfg, w->cell_scale, *scene, h);
   if (st) return st;
   cudaStreamSynchronize(w->st());
   w->drop_graphs();
@@ -1660,6 +1663,49 @@ int blobs_world_drain_events(blobs_world* w, uint32_t* col_a, uint32_t* col_b, f
   *n_written = k;
   if (n_left) *n_left = w->ev_host.size();
   return read_status(w);
+}
+
+int blobs_world_autotune(blobs_world* w, const blobs_scene* scene, float old_dt, double delta, uint32_t trial_steps,
+                         float* cell_scale) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!scene || trial_steps == 0 || !(delta > 0.0)) return BLOBS_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  // every cell edge >= the smallest exact one gives the same contacts in the
+  // same order, so the choice only changes the time
+  static const float kScales[] = {1.0f, 1.125f, 1.25f, 1.5f, 1.75f};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best_ms = INFINITY, best = 1.0f;
+  int status = BLOBS_OK;
+  for (float sc : kScales) {
+    w->cell_scale = sc;
+    status = blobs_world_load(w, scene, old_dt);
+    if (status) break;
+    status = run_steps(w, delta, 2);  // the irregular first step, graph capture
+    if (!status) status = run_steps(w, delta, trial_steps);  // captures the trial graph
+    if (status) break;
+    e = cudaEventRecord(e0, w->st());
+    if (e == cudaSuccess) status = run_steps(w, delta, trial_steps);
+    if (e == cudaSuccess && !status) e = cudaEventRecord(e1, w->st());
+    if (e == cudaSuccess && !status) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess && !status) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) status = blobs_map_cuda(e);
+    if (!status) status = read_status(w);
+    if (status) break;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = sc;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  w->cell_scale = best;
+  if (status) return status;
+  if (cell_scale) *cell_scale = best;
+  return blobs_world_load(w, scene, old_dt);  // the scene's initial state, tuned grid
 }
 
 int blobs_world_kernel_launches(blobs_world* w, uint64_t* count) {

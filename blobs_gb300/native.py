@@ -106,6 +106,7 @@ def lib() -> ctypes.CDLL:
         "blobs_world_kernel_launches": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_phase_times": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(u64), u32]),
         "blobs_world_set_events": (i32, [_P, i32, u32]),
+        "blobs_world_autotune": (i32, [_P, ctypes.POINTER(SceneStruct), f32, f64, u32, ctypes.POINTER(f32)]),
         "blobs_spatial_hash_create": (i32, [f32, i32, pp]),
         "blobs_spatial_hash_destroy": (i32, [_P]),
         "blobs_spatial_hash_set_points": (i32, [_P, u64, _P, _P, _P]),
@@ -196,6 +197,25 @@ class World:
         self.close()
 
     def load(self, scene: scenes.Scene, old_dt: float = 1.0) -> None:
+        st, keep = self._scene_struct(scene)
+        check(lib().blobs_world_load(self._h, ctypes.byref(st), float(old_dt)), "blobs_world_load")
+        self.n_bodies = scene.n_bodies
+        self.n_colliders = scene.n_colliders
+        self.n_joints = scene.n_joints
+
+    def autotune(self, scene: scenes.Scene, dt: float, trial_steps: int = 5, old_dt: float = 1.0) -> float:
+        """Time a few broadphase cell edges on `scene`, keep the fastest and
+        reload the scene with it; returns the chosen scale."""
+        st, keep = self._scene_struct(scene)
+        scale = ctypes.c_float()
+        check(lib().blobs_world_autotune(self._h, ctypes.byref(st), float(old_dt), float(dt), int(trial_steps),
+                                         ctypes.byref(scale)), "blobs_world_autotune")
+        self.n_bodies = scene.n_bodies
+        self.n_colliders = scene.n_colliders
+        self.n_joints = scene.n_joints
+        return float(scale.value)
+
+    def _scene_struct(self, scene: scenes.Scene):
         keep = []
 
         def arr(a, dtype):
@@ -253,10 +273,7 @@ class World:
         st.jnt_target = arr(scene.jnt_target, np.float32)
         st.n_circles = int(scene.circles.shape[0])
         st.circles = arr(scene.circles, np.float32)
-        check(lib().blobs_world_load(self._h, ctypes.byref(st), float(old_dt)), "blobs_world_load")
-        self.n_bodies = scene.n_bodies
-        self.n_colliders = scene.n_colliders
-        self.n_joints = scene.n_joints
+        return st, keep
 
     def step(self, dt: float) -> None:
         check(lib().blobs_world_step(self._h, float(dt)), "blobs_world_step")

@@ -254,6 +254,17 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
  * BLOBS_OK.  Synchronising. */
 int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk);
 
+/* Autotuner (no counterpart in the reference): loads `scene` with each of a
+ * few broadphase cell edges (1, 1.125, 1.25, 1.5 and 1.75 times the smallest
+ * exact edge, 2 x largest radius x (1 + 1/64)), times `trial_steps` steps
+ * of `delta` from the scene's initial state on the world's stream, keeps the
+ * fastest (*cell_scale, may be NULL) and reloads the scene with it.  Every
+ * such edge gives the same contacts in the same order: the results do not
+ * depend on the choice.  A later blobs_world_load keeps the chosen scale.
+ * Synchronising. */
+int blobs_world_autotune(blobs_world* w, const blobs_scene* scene, float old_dt, double delta, uint32_t trial_steps,
+                         float* cell_scale);
+
 /* ---- collision events -------------------------------------------------------- */
 
 /* Replaces the CollisionEvent channel (lib.rs:146-153): Physics::new's
