@@ -251,6 +251,39 @@ def batched_comparison(dev, steps=100, sample=256, seed=4):
                       % (sample, bodies)}
 
 
+def general_comparison(dev, steps=10, warmup=3, seed=3):
+    """Configuration 3 on the general path: 200,000 bodies with 1-4 sphere
+    colliders each, 50,000 fixed joints (coloured Gauss-Seidel, 4
+    iterations), 100,000 damped springs, box 1500 x 1500, dt = 1/120.
+    Device time of `steps` single steps after `warmup`, L2 flushed before
+    each, on the world's stream."""
+    import torch
+    from blobs_gb300 import native, scenes
+    scene = scenes.config3(seed=seed)
+    stream = torch.cuda.current_stream(dev)
+    w = native.World(scene, device=dev.index)
+    w.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        w.step(scene.dt)
+    torch.cuda.synchronize()
+    k0 = w.kernel_launches()
+    ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.step(scene.dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    launches = (w.kernel_launches() - k0) / steps
+    w.close()
+    return {"bodies": scene.n_bodies, "colliders": scene.n_colliders, "joints": scene.n_joints,
+            "springs": scene.n_springs, "steps": steps, "ms_per_step": ms / steps,
+            "body_steps_per_s": scene.n_bodies * steps / (ms / 1e3), "kernel_launches_per_step": launches}
+
+
 def adjoint_comparison(dev, steps=120, every=16, seed=5):
     """Configuration 5: 256 worlds x 2,048 spheres with 1,024 springs each,
     a 120-step forward pass (one CUDA-graph rollout) against the same
@@ -427,6 +460,8 @@ def run_ours(args):
         line["batched"] = batched_comparison(dev)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_comparison(dev)
+    if rank == 0 and not args.no_general:
+        line["general"] = general_comparison(dev)
     world.close()
     if dist is not None:
         dist.barrier()
@@ -445,6 +480,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-general", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -616,8 +616,8 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     mark_begin(w, PHASE_JOINTS);
     for (uint32_t it = 0; it < w->cfg.joint_iterations; ++it)
       for (size_t k = 0; k < n_colours; ++k) launch_joints(d, p, w->colour_offsets[k], w->colour_offsets[k + 1], dt, st);
-    mark_end(w);
     w->enqueued += (uint64_t)w->cfg.joint_iterations * n_colours;
+    mark_end(w);
   };
   if (w->sorted_storage) {
     // the first substep of a step re-sorts the body storage into cell order;
@@ -787,7 +787,10 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
     w->graph_cur_after[key] = w->cur;
     w->enqueued = before;
     e = cudaStreamEndCapture(w->st(), &g);
-    if (e != cudaSuccess) return blobs_map_cuda(e);
+    if (e != cudaSuccess) {
+      w->cur = cur0;  // nothing ran
+      return blobs_map_cuda(e);
+    }
     cudaGraphExec_t ge = nullptr;
     e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
