@@ -3,6 +3,9 @@
 //   physics_host_test scene IN OUT STEPS DT    build a world through the Physics API the way the
 //                                              reference demo does (demo/src/simulation.rs:99-146),
 //                                              step it on the GPU, write the body state
+//   physics_host_test mutate IN OUT S1 S2 DT K  the same world: S1 steps, then remove_rbd of every
+//                                              K-th body and remove_col of the collider of every
+//                                              K-th body after it (physics.rs:159-172), S2 steps
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -143,15 +146,74 @@ static int scene_test(const char* in, const char* out, int steps, double dt) {
   return 0;
 }
 
+// IN as for scene_test.  OUT: the state of every body after S1 steps (pos,
+// pos_old, vel, snapshot: 8 floats), then the state of the remaining bodies
+// after S2 more steps (same 8 floats each).
+static int mutate_test(const char* in, const char* out, int s1, int s2, double dt, int every) {
+  FILE* f = std::fopen(in, "rb");
+  if (!f) return 2;
+  uint32_t n;
+  float g[2], box[4];
+  if (std::fread(&n, 4, 1, f) != 1 || std::fread(g, 4, 2, f) != 2 || std::fread(box, 4, 4, f) != 4) return 2;
+  Physics p(Vec2(g[0], g[1]));
+  p.walls = std::make_pair(Vec2(box[0], box[1]), Vec2(box[2], box[3]));
+  std::vector<RigidBodyHandle> hs;
+  std::vector<ColliderHandle> cs;
+  for (uint32_t i = 0; i < n; ++i) {
+    float rec[5];
+    uint8_t type;
+    if (std::fread(rec, 4, 5, f) != 5 || std::fread(&type, 1, 1, f) != 1) return 2;
+    RigidBodyHandle h = p.insert_rbd(RigidBodyBuilder()
+                                         .position(Vec2(rec[0], rec[1]))
+                                         .velocity_request(Vec2(rec[2], rec[3]))
+                                         .body_type((RigidBodyType)type)
+                                         .build());
+    cs.push_back(p.insert_collider_with_parent(
+        ColliderBuilder().radius(rec[4]).absolute_translation(Vec2(rec[0], rec[1])).build(), h));
+    hs.push_back(h);
+  }
+  std::fclose(f);
+  FILE* o = std::fopen(out, "wb");
+  auto dump = [&](uint32_t i) {
+    const RigidBody* b = p.get_rbd(hs[i]);
+    const Collider* c = p.get_col(cs[i]);
+    float rec[8] = {b->position.x, b->position.y, b->position_old.x, b->position_old.y,
+                    b->calculated_velocity.x, b->calculated_velocity.y, c->absolute_translation.x,
+                    c->absolute_translation.y};
+    std::fwrite(rec, 4, 8, o);
+  };
+  for (int s = 0; s < s1; ++s) p.step(dt);
+  for (uint32_t i = 0; i < n; ++i) dump(i);
+  std::vector<bool> gone(n, false);
+  for (uint32_t i = 0; i < n; i += (uint32_t)every) {
+    p.remove_rbd(hs[i]);
+    gone[i] = true;
+    if (i + 1 < n) {
+      p.remove_col(cs[i + 1]);  // the body's last collider: the body goes too
+      gone[i + 1] = true;
+    }
+  }
+  for (int s = 0; s < s2; ++s) p.step(dt);
+  for (uint32_t i = 0; i < n; ++i) {
+    EXPECT(gone[i] == (p.get_rbd(hs[i]) == nullptr));
+    if (!gone[i]) dump(i);
+  }
+  std::fclose(o);
+  return failures ? 1 : 0;
+}
+
 int main(int argc, char** argv) {
   try {
     if (argc >= 2 && std::strcmp(argv[1], "cpu") == 0) return cpu_tests();
     if (argc >= 6 && std::strcmp(argv[1], "scene") == 0)
       return scene_test(argv[2], argv[3], std::atoi(argv[4]), std::atof(argv[5]));
+    if (argc >= 8 && std::strcmp(argv[1], "mutate") == 0)
+      return mutate_test(argv[2], argv[3], std::atoi(argv[4]), std::atoi(argv[5]), std::atof(argv[6]),
+                         std::atoi(argv[7]));
   } catch (const Error& e) {
     std::fprintf(stderr, "blobs error: %s\n", e.what());
     return 3;
   }
-  std::fprintf(stderr, "usage: %s cpu | scene IN OUT STEPS DT\n", argv[0]);
+  std::fprintf(stderr, "usage: %s cpu | scene IN OUT STEPS DT | mutate IN OUT S1 S2 DT K\n", argv[0]);
   return 2;
 }

@@ -69,3 +69,53 @@ def test_host_mirror_steps_bit_exact(host_test_bin, tmp_path):
     np.testing.assert_array_equal(ev_ids[:, 1], b)
     np.testing.assert_array_equal(ev_vel[:, 0:2].astype(np.float64), va)
     np.testing.assert_array_equal(ev_vel[:, 2:4].astype(np.float64), vb)
+
+
+@pytest.mark.gpu
+def test_host_mirror_remove_and_continue(host_test_bin, tmp_path):
+    """Host mutation round trip through the C++ mirror: step, remove bodies
+    (remove_rbd) and last colliders (remove_col, which takes the body with
+    it), step again.  Both phases equal the oracle bit for bit; the second
+    phase is the oracle restarted from the first phase's state without the
+    removed bodies (arena iteration skips the freed slots)."""
+    s = scenes.config1(seed=19, n=600)
+    inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    with open(inp, "wb") as f:
+        np.array([s.n_bodies], np.uint32).tofile(f)
+        s.gravity.astype(np.float32).tofile(f)
+        s.world_box[0].astype(np.float32).tofile(f)
+        for i in range(s.n_bodies):
+            np.array([s.pos[i, 0], s.pos[i, 1], s.vreq[i, 0], s.vreq[i, 1], s.col_radius[i]], np.float32).tofile(f)
+            np.array([s.body_type[i]], np.uint8).tofile(f)
+    s1, s2, every = 10, 12, 7
+    r = subprocess.run([host_test_bin, "mutate", inp, outp, str(s1), str(s2), repr(s.dt), str(every)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = np.frombuffer(open(outp, "rb").read(), np.float32).reshape(-1, 8)
+    first, second = raw[:s.n_bodies], raw[s.n_bodies:]
+    o = oracle.OracleWorld(s, 32)
+    assert o.step(s.dt, s1) == 0
+    b = o.bodies()
+    snap = o.snapshots()
+    np.testing.assert_array_equal(first[:, 0:2].astype(np.float64), b["pos"])
+    np.testing.assert_array_equal(first[:, 2:4].astype(np.float64), b["pos_old"])
+    np.testing.assert_array_equal(first[:, 4:6].astype(np.float64), b["vel"])
+    np.testing.assert_array_equal(first[:, 6:8].astype(np.float64), snap)
+    keep = np.ones(s.n_bodies, bool)
+    for i in range(0, s.n_bodies, every):
+        keep[i] = False
+        if i + 1 < s.n_bodies:
+            keep[i + 1] = False
+    idx = np.flatnonzero(keep)
+    rest = scenes.spheres(b["pos"][idx], s.col_radius[idx], box=tuple(s.world_box[0]),
+                          body_type=s.body_type[idx])
+    rest.pos_old = b["pos_old"][idx]
+    rest.vel = b["vel"][idx]
+    rest.col_snap = snap[idx]
+    o2 = oracle.OracleWorld(rest, 32, old_dt=float(np.float32(np.float32(s.dt) / np.float32(8))))
+    assert o2.step(s.dt, s2) == 0
+    b2 = o2.bodies()
+    assert second.shape[0] == len(idx)
+    np.testing.assert_array_equal(second[:, 0:2].astype(np.float64), b2["pos"])
+    np.testing.assert_array_equal(second[:, 2:4].astype(np.float64), b2["pos_old"])
+    np.testing.assert_array_equal(second[:, 4:6].astype(np.float64), b2["vel"])
