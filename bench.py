@@ -117,7 +117,7 @@ def cpu_baseline(sizes=(4096, 8192, 16384, 32768), target_n=1_000_000, seed=2, s
     from oracle import oracle
     ns, ts = [], []
     for n in sizes:
-        s = scenes.config2(seed=seed, n=n)
+        s = scenes.dense_spheres(seed=seed, n=n)
         w = oracle.OracleWorld(s, 32, maintain_spatial_hash=True)
         w.time_steps(s.dt, 1)  # first step: pending velocity requests
         t = w.time_steps(s.dt, steps_per_size) / steps_per_size
@@ -168,7 +168,7 @@ def run_reference(args):
     ns, ts = [], []
     for i in range(args.warmup + args.steps):
         n = sizes[i % len(sizes)]
-        s = scenes.config2(seed=2, n=n)
+        s = scenes.dense_spheres(seed=2, n=n)
         w = oracle.OracleWorld(s, 32, maintain_spatial_hash=True)
         w.time_steps(s.dt, 1)
         t = w.time_steps(s.dt, 1)
@@ -184,7 +184,7 @@ def run_reference(args):
         "impl": "reference", "metric": "sphere-steps/s @1M", "value": value, "unit": "sphere-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_target * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded config2 generator)",
+        "data": "synthetic (seeded dense_spheres generator)",
         "config": {"workload": "1M spheres, r~U[0.05,0.15], 40% packing, dt=1/120, 8 substeps (extrapolated from "
                                "samples)", "bodies": N},
         "cpu_baseline": {"value": value, "unit": "sphere-steps/s", "cores": 1, "kind": "port",
@@ -199,14 +199,14 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 def batched_comparison(dev, steps=100, sample=256, seed=4):
-    """Configuration 4: 4,096 uneven worlds stepped as one batch (a 100-step
+    """4,096 uneven worlds stepped as one batch (a 100-step
     rollout captured in one CUDA graph) against the per-world form (each
     world its own device world and its own 100-step rollout launch), timed on
     `sample` evenly spaced worlds and scaled to all 4,096 by body count."""
     import numpy as np
     import torch
     from blobs_gb300 import native, scenes
-    scene = scenes.config4(seed=seed, steps=steps)
+    scene = scenes.uneven_batch(seed=seed, steps=steps)
     dt = scene.dt
     stream = torch.cuda.current_stream(dev)
     w = native.World(scene, device=dev.index)
@@ -252,14 +252,14 @@ def batched_comparison(dev, steps=100, sample=256, seed=4):
 
 
 def general_comparison(dev, steps=10, warmup=3, seed=3):
-    """Configuration 3 on the general path: 200,000 bodies with 1-4 sphere
+    """The general path: 200,000 bodies with 1-4 sphere
     colliders each, 50,000 fixed joints (coloured Gauss-Seidel, 4
     iterations), 100,000 damped springs, box 1500 x 1500, dt = 1/120.
     Device time of `steps` single steps after `warmup`, L2 flushed before
     each, on the world's stream."""
     import torch
     from blobs_gb300 import native, scenes
-    scene = scenes.config3(seed=seed)
+    scene = scenes.jointed_bodies(seed=seed)
     stream = torch.cuda.current_stream(dev)
     w = native.World(scene, device=dev.index)
     w.set_stream(stream.cuda_stream)
@@ -285,7 +285,7 @@ def general_comparison(dev, steps=10, warmup=3, seed=3):
 
 
 def adjoint_comparison(dev, steps=120, every=16, seed=5):
-    """Configuration 5: 256 worlds x 2,048 spheres with 1,024 springs each,
+    """256 worlds x 2,048 spheres with 1,024 springs each,
     a 120-step forward pass (one CUDA-graph rollout) against the same
     rollout recorded with a checkpoint every 16 steps plus the backward pass
     (recompute each segment, then the adjoint substeps in reverse).  Timed
@@ -294,7 +294,7 @@ def adjoint_comparison(dev, steps=120, every=16, seed=5):
     import numpy as np
     import torch
     from blobs_gb300 import native, scenes
-    scene, marked, targets = scenes.config5(seed=seed, steps=steps)
+    scene, marked, targets = scenes.gradient_batch(seed=seed, steps=steps)
     dt = scene.dt
     stream = torch.cuda.current_stream(dev)
     w = native.World(scene, device=dev.index)
@@ -355,7 +355,7 @@ def run_ours(args):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
 
-    scene = scenes.config2(seed=2 + rank, n=args.n)
+    scene = scenes.dense_spheres(seed=2 + rank, n=args.n)
     dt = scene.dt
     world = native.World(scene, device=local_rank)
     stream = torch.cuda.Stream(dev)          # graphs cannot be captured on the legacy default stream
@@ -436,7 +436,7 @@ def run_ours(args):
         "metric": "sphere-steps/s @1M", "value": value, "unit": "sphere-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded config2 generator: uniform positions with overlaps, N(0,0.5) velocities)",
+        "data": "synthetic (seeded dense_spheres generator: uniform positions with overlaps, N(0,0.5) velocities)",
         "config": {"workload": "1M spheres, r~U[0.05,0.15], 40%% packing (side %.1f, walled), g=(0,-9.81), "
                                "dt=1/120, 8 substeps/step" % (float(scene.world_box[0, 2] * 2)),
                    "bodies": scene.n_bodies, "substeps": scene.substeps, "parallelism": "replicas" if world_size > 1

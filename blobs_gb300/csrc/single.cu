@@ -1,6 +1,6 @@
 // single.cu -- the single-sphere path: every body owns exactly one collider
 // at offset zero with default groups and no sensor, and there are no fixed
-// joints (configurations 1, 2, 4 and 5).
+// joints (sparse and dense sphere worlds, uneven batches, the gradient batch).
 //
 // Body state lives in "storage order", re-sorted into cell order once per
 // step, so that a warp's bodies are spatial neighbours:

@@ -239,18 +239,18 @@ def box_side(n: int, rmin: float, rmax: float, packing: float) -> float:
     return math.sqrt(n * math.pi * er2 / packing)
 
 
-def config1(seed: int = 1, n: int = 1000, steps: int = 600) -> Scene:
+def sparse_spheres(seed: int = 1, n: int = 1000, steps: int = 600) -> Scene:
     """1,000 single-sphere bodies, r ~ U[0.1, 0.3], non-overlapping in a 40x40
     walled box, v ~ N(0, 1) per axis, g = (0, -9.81), dt = 1/60, 600 steps."""
     rng = np.random.Generator(np.random.PCG64(seed))
     pos, rad = _nonoverlapping(rng, n, 0.1, 0.3, -20.0, 20.0)
     vel = rng.normal(0.0, 1.0, (n, 2)).astype(np.float32)
     s = spheres(pos, rad, vel, box=(-20.0, -20.0, 20.0, 20.0))
-    s.dt, s.n_steps, s.name, s.seed = 1.0 / 60.0, steps, "config1-1k-walled", seed
+    s.dt, s.n_steps, s.name, s.seed = 1.0 / 60.0, steps, "sparse_spheres-1k-walled", seed
     return s
 
 
-def config2(seed: int = 2, n: int = 1_000_000, steps: int = 1000, literal_box: bool = False) -> Scene:
+def dense_spheres(seed: int = 2, n: int = 1_000_000, steps: int = 1000, literal_box: bool = False) -> Scene:
     """1M single-sphere bodies, r ~ U[0.05, 0.15], uniform with overlaps in a
     walled square box at 40% packing (side 291.7 for 1M; the literal 2000x2000
     box of the workload text is 0.85% packing and is kept as `literal_box`),
@@ -264,7 +264,7 @@ def config2(seed: int = 2, n: int = 1_000_000, steps: int = 1000, literal_box: b
     vel = rng.normal(0.0, 0.5, (n, 2)).astype(np.float32)
     s = spheres(pos, rad, vel, box=(-h, -h, h, h))
     s.dt, s.n_steps, s.seed = 1.0 / 120.0, steps, seed
-    s.name = "config2-%d-%s" % (n, "2000box" if literal_box else "40pct")
+    s.name = "dense_spheres-%d-%s" % (n, "2000box" if literal_box else "40pct")
     return s
 
 
@@ -280,7 +280,7 @@ def _pairs_within(pos, radius_max, rng=None):
     return pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
 
 
-def config3(seed: int = 3, n: int = 200_000, n_joints: int = 50_000, n_springs: int = 100_000,
+def jointed_bodies(seed: int = 3, n: int = 200_000, n_joints: int = 50_000, n_springs: int = 100_000,
             side: float = 1500.0, steps: int = 500) -> Scene:
     """200k bodies with 1-4 sphere colliders at offsets uniform in a disc of
     radius 0.5, r ~ U[0.1, 0.25]; 50k fixed joints between random body pairs
@@ -320,7 +320,7 @@ def config3(seed: int = 3, n: int = 200_000, n_joints: int = 50_000, n_springs: 
     cdamp = rng.uniform(0.0, 2.0, len(sp)).astype(np.float32)
     add_springs(s, sp[:, 0], sp[:, 1], k, cdamp)
     s.world_box = np.array([[-h, -h, h, h]], np.float32)
-    s.dt, s.n_steps, s.name, s.seed = 1.0 / 120.0, steps, "config3-%d-structured" % n, seed
+    s.dt, s.n_steps, s.name, s.seed = 1.0 / 120.0, steps, "jointed_bodies-%d-structured" % n, seed
     return s
 
 
@@ -424,7 +424,7 @@ def unpack_world(s: Scene, w: int) -> Scene:
     return out
 
 
-def config4(seed: int = 4, n_worlds: int = 4096, nmin: int = 64, nmax: int = 8192, steps: int = 100) -> Scene:
+def uneven_batch(seed: int = 4, n_worlds: int = 4096, nmin: int = 64, nmax: int = 8192, steps: int = 100) -> Scene:
     """4,096 independent worlds, body counts log-uniform in [64, 8192],
     single spheres r ~ U[0.1, 0.3] at 35% packing in their own walled box,
     v ~ N(0, 1); 10% of each world's bodies get a spring (k = 200, c = 1,
@@ -435,11 +435,11 @@ def config4(seed: int = 4, n_worlds: int = 4096, nmin: int = 64, nmax: int = 819
     worlds = [random_world(rng, int(c), 0.1, 0.3, 0.35, 1.0, spring_frac=0.10) for c in counts]
     s = pack(worlds)
     s.dt, s.n_steps, s.seed = 1.0 / 60.0, steps, seed
-    s.name = "config4-%dworlds-%dbodies" % (n_worlds, s.n_bodies)
+    s.name = "uneven_batch-%dworlds-%dbodies" % (n_worlds, s.n_bodies)
     return s
 
 
-def config5(seed: int = 5, n_worlds: int = 256, n_per: int = 2048, n_springs: int = 1024, steps: int = 120,
+def gradient_batch(seed: int = 5, n_worlds: int = 256, n_per: int = 2048, n_springs: int = 1024, steps: int = 120,
             n_marked: int = 64):
     """256 worlds x 2,048 spheres, r ~ U[0.1, 0.2] at 30% packing (walled box,
     side 22.4), 1,024 springs per world between random nearby pairs with
@@ -462,5 +462,5 @@ def config5(seed: int = 5, n_worlds: int = 256, n_per: int = 2048, n_springs: in
         targets.append(s.pos[m] + rng.normal(0.0, 1.0, (n_marked, 2)).astype(np.float32))
     s = pack(worlds)
     s.dt, s.n_steps, s.seed = 1.0 / 60.0, steps, seed
-    s.name = "config5-%dx%d" % (n_worlds, n_per)
+    s.name = "gradient_batch-%dx%d" % (n_worlds, n_per)
     return s, marked, targets

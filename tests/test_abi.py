@@ -51,7 +51,7 @@ def test_config_defaults_match_physics_new():
 
 @pytest.mark.parametrize("seed", [0, 1])
 def test_mass_inertia_matches_oracle(seed):
-    s = scenes.config3(seed=seed, n=3000, n_joints=100, n_springs=100, side=60.0)
+    s = scenes.jointed_bodies(seed=seed, n=3000, n_joints=100, n_springs=100, side=60.0)
     s.col_sensor[::7] = 1
     s.col_mass_override[::5] = 0.75
     m, I = native.mass_inertia(s)

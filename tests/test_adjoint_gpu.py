@@ -133,7 +133,7 @@ def test_config5_worlds_short_horizon_match_replay():
     orders of magnitude every few steps (max |dL/dv0| of one world: 4e-2 at
     step 10, 1e1 at 15, 1e12 at 40, 1e84 at 120, in f64) and leaves the f32
     range, so the check is made where it is finite."""
-    scene, marked, targets = scenes.config5()
+    scene, marked, targets = scenes.gradient_batch()
     steps = 10
     final, g, after, gv, gk = gpu_gradients(scene, marked, targets, steps, 4)
     assert np.array_equal(final, after)

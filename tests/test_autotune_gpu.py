@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_autotuned_single_world_matches_oracle():
-    s = scenes.config1(seed=61, n=3000)
+    s = scenes.sparse_spheres(seed=61, n=3000)
     with native.World(s) as w:
         cs0 = w.grid()[0]
         scale = w.autotune(s, s.dt, trial_steps=3)
@@ -34,7 +34,7 @@ def test_autotuned_single_world_matches_oracle():
 def test_every_candidate_edge_gives_the_same_rollout(scale):
     """Each scale the autotuner may choose, forced through a requested cell
     edge, reproduces the default rollout of a batched spring world."""
-    s = scenes.config4(seed=62, n_worlds=24, nmin=64, nmax=1500, steps=5)
+    s = scenes.uneven_batch(seed=62, n_worlds=24, nmin=64, nmax=1500, steps=5)
     with native.World(s) as w:
         w.rollout(s.dt, 12)
         want = w.read_bodies()

@@ -41,7 +41,7 @@ def cpu_candidates(snap, inv_cs, origin, log2w, log2h):
 
 @pytest.mark.parametrize("n,literal", [(5000, False), (20000, True)])
 def test_candidate_pairs_bit_exact(n, literal):
-    s = scenes.config2(seed=40 + n, n=n, literal_box=literal)
+    s = scenes.dense_spheres(seed=40 + n, n=n, literal_box=literal)
     with native.World(s) as w:
         w.step(s.dt)
         snap = w.read_snapshots()
@@ -55,7 +55,7 @@ def test_candidate_pairs_bit_exact(n, literal):
 def test_contact_pairs_equal_bruteforce():
     """The contact subset equals the reference's O(C^2) brute-force contact set
     (groups, parents and dist < ra + rb) on the same snapshots."""
-    s = scenes.config3(seed=41, n=4000, n_joints=0, n_springs=0, side=70.0)
+    s = scenes.jointed_bodies(seed=41, n=4000, n_joints=0, n_springs=0, side=70.0)
     s.jnt_a = s.jnt_a[:0]
     rng = np.random.Generator(np.random.PCG64(41))
     s.col_memb = rng.choice(np.array([1, 2, 0xFFFFFFFF], np.uint32), s.n_colliders)
@@ -75,7 +75,7 @@ def test_emit_pairs_overflow_then_retry():
     """An undersized buffer reports BLOBS_ERR_OVERFLOW with the full count; a
     retry with that capacity succeeds (host-side fault injection)."""
     import ctypes
-    s = scenes.config2(seed=42, n=3000)
+    s = scenes.dense_spheres(seed=42, n=3000)
     with native.World(s) as w:
         n = ctypes.c_uint64()
         buf = np.zeros((4, 2), np.uint32)

@@ -58,7 +58,7 @@ def gpu_events(scene, steps, dt, rollout=False, capacity=1 << 20):
 
 @pytest.mark.parametrize("rollout", [False, True])
 def test_events_single_spheres(rollout):
-    s = scenes.config1(seed=41, n=400)
+    s = scenes.sparse_spheres(seed=41, n=400)
     got, pos = gpu_events(s, 6, s.dt, rollout=rollout)
     assert_same_events(got, oracle_events(s, 6, s.dt))
 
@@ -72,7 +72,7 @@ def test_events_with_springs_and_walls():
 
 
 def test_events_multi_collider_sensors_groups():
-    s = scenes.config3(seed=43, n=3000, n_joints=0, n_springs=500, side=60.0)
+    s = scenes.jointed_bodies(seed=43, n=3000, n_joints=0, n_springs=500, side=60.0)
     rng = np.random.Generator(np.random.PCG64(43))
     s.col_sensor = (rng.random(s.n_colliders) < 0.1).astype(np.uint8)
     s.col_memb = rng.choice(np.array([1, 2, 0xFFFFFFFF], np.uint32), s.n_colliders)
@@ -97,7 +97,7 @@ def test_events_batched_worlds():
 
 
 def test_events_enabled_mid_run_and_partial_drains():
-    s = scenes.config1(seed=45, n=400)
+    s = scenes.sparse_spheres(seed=45, n=400)
     with native.World(s) as w:
         for _ in range(3):
             w.step(s.dt)  # velocities kept as displacements until events are on
@@ -129,7 +129,7 @@ def test_events_overflow_drops_the_batch_and_reports_the_count():
 
 
 def test_drain_without_events_is_a_state_error():
-    s = scenes.config1(seed=47, n=50)
+    s = scenes.sparse_spheres(seed=47, n=50)
     with native.World(s) as w:
         with pytest.raises(native.BlobsError) as ei:
             w.drain_events()

@@ -34,7 +34,7 @@ def test_host_mirror_steps_bit_exact(host_test_bin, tmp_path):
     """A world inserted body by body through Physics::insert_rbd /
     insert_collider_with_parent and stepped through Physics::step equals the
     oracle bit for bit."""
-    s = scenes.config1(seed=17, n=400)
+    s = scenes.sparse_spheres(seed=17, n=400)
     s.body_type[::37] = scenes.STATIC
     inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
     with open(inp, "wb") as f:
@@ -78,7 +78,7 @@ def test_host_mirror_remove_and_continue(host_test_bin, tmp_path):
     it), step again.  Both phases equal the oracle bit for bit; the second
     phase is the oracle restarted from the first phase's state without the
     removed bodies (arena iteration skips the freed slots)."""
-    s = scenes.config1(seed=19, n=600)
+    s = scenes.sparse_spheres(seed=19, n=600)
     inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
     with open(inp, "wb") as f:
         np.array([s.n_bodies], np.uint32).tofile(f)

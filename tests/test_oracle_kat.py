@@ -165,7 +165,7 @@ def test_pushout_coincident_spheres():
 
 
 def test_f32_close_to_f64_one_substep():
-    s = scenes.config1(seed=3, n=200)
+    s = scenes.sparse_spheres(seed=3, n=200)
     w32 = _one_substep(s)
     w64 = oracle.OracleWorld(s.copy(), 64)
     s64 = s.copy()
@@ -176,7 +176,7 @@ def test_f32_close_to_f64_one_substep():
 
 
 def test_contact_pairs_bruteforce_matches_step_count():
-    s = scenes.config2(seed=9, n=2000, steps=1)
+    s = scenes.dense_spheres(seed=9, n=2000, steps=1)
     i, j = oracle.contact_pairs(s.pos, s.col_radius)
     s1 = s.copy()
     s1.substeps = 1

@@ -46,10 +46,10 @@ def assert_exact(got, want, keys=("pos", "pos_old", "vel")):
             k, len(bad), bad[:3].tolist(), g[tuple(bad[0])], want[k][tuple(bad[0])])
 
 
-# ---- configuration 1: 1,000 spheres in a walled box -------------------------
+# ---- 1,000 spheres in a walled box ---------------------------------------------
 
 def test_config1_single_step_bit_exact():
-    s = scenes.config1()
+    s = scenes.sparse_spheres()
     got, want = run_gpu(s, 1), run_oracle(s, 1)
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
     assert got["contacts"] == want["contacts"]
@@ -58,7 +58,7 @@ def test_config1_single_step_bit_exact():
 def test_config1_full_600_step_rollout_bit_exact():
     """All 600 steps (4,800 substeps): a single differing bit anywhere would
     grow chaotically, so equality at the end pins every substep."""
-    s = scenes.config1()
+    s = scenes.sparse_spheres()
     got, want = run_gpu(s, s.n_steps), run_oracle(s, s.n_steps)
     assert want["pushouts"] == 0
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
@@ -66,7 +66,7 @@ def test_config1_full_600_step_rollout_bit_exact():
 
 
 def test_rollout_graph_equals_eager_steps():
-    s = scenes.config1(seed=11, n=500)
+    s = scenes.sparse_spheres(seed=11, n=500)
     a = run_gpu(s, 40)
     with native.World(s) as w:
         w.step(s.dt)
@@ -76,17 +76,17 @@ def test_rollout_graph_equals_eager_steps():
 
 
 def test_determinism_two_runs_bitwise_equal():
-    s = scenes.config2(seed=5, n=20000)
+    s = scenes.dense_spheres(seed=5, n=20000)
     a, b = run_gpu(s, 5), run_gpu(s, 5)
     for k in ("pos", "pos_old", "vel"):
         assert np.array_equal(a[k], b[k])
 
 
-# ---- configuration 2 (scaled): dense overlapping spheres ---------------------
+# ---- dense overlapping spheres (scaled down) --------------------------------
 
 @pytest.mark.parametrize("n", [4096, 30000])
 def test_config2_scaled_bit_exact(n):
-    s = scenes.config2(seed=2, n=n)
+    s = scenes.dense_spheres(seed=2, n=n)
     got, want = run_gpu(s, 3), run_oracle(s, 3)
     assert want["pushouts"] == 0
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
@@ -96,7 +96,7 @@ def test_config2_scaled_bit_exact(n):
 def test_config1_f64_tolerance():
     """Sparse non-overlapping world: one step within |dx| <= 1e-4 (1 + |x|) of
     the f64 re-run, every component."""
-    s = scenes.config1(seed=21)
+    s = scenes.sparse_spheres(seed=21)
     got, want = run_gpu(s, 1), run_oracle(s, 1, precision=64)
     err = np.abs(got["pos"].astype(np.float64) - want["pos"])
     assert np.all(err <= 1e-4 * (1.0 + np.abs(want["pos"]))), err.max()
@@ -108,7 +108,7 @@ def test_config2_f64_tolerance():
     from f64 by up to ~1e-2 after 8 substeps, median ~1e-6).  Stated
     tolerance: 99% of components within 1e-4 (1 + |x|) of f64, and the GPU's
     largest deviation no larger than the f32 reference's own."""
-    s = scenes.config2(seed=21, n=4096)
+    s = scenes.dense_spheres(seed=21, n=4096)
     got, want = run_gpu(s, 1), run_oracle(s, 1, precision=64)
     ref32 = run_oracle(s, 1, precision=32)
     err = np.abs(got["pos"].astype(np.float64) - want["pos"])
@@ -118,7 +118,7 @@ def test_config2_f64_tolerance():
 
 
 def test_literal_2000_box_bit_exact():
-    s = scenes.config2(seed=8, n=20000, literal_box=True)
+    s = scenes.dense_spheres(seed=8, n=20000, literal_box=True)
     got, want = run_gpu(s, 2), run_oracle(s, 2)
     assert_exact(got, want)
 
@@ -134,7 +134,7 @@ def test_springs_bit_exact():
 
 
 def test_static_bodies_sensors_groups_bit_exact():
-    s = scenes.config2(seed=31, n=5000)
+    s = scenes.dense_spheres(seed=31, n=5000)
     rng = np.random.Generator(np.random.PCG64(31))
     s.body_type[rng.random(s.n_bodies) < 0.1] = scenes.STATIC
     s.col_sensor[rng.random(s.n_colliders) < 0.05] = 1
@@ -150,7 +150,7 @@ def test_multi_collider_bodies_bit_exact():
     """Config 3 layout without joints: rotation stays 0, so the snapshots
     (rot(0) * offset + p) are exact and the merged per-body contact order is
     the reference's (outer collider, inner collider) sequence."""
-    s = scenes.config3(seed=3, n=6000, n_joints=0, n_springs=2000, side=90.0)
+    s = scenes.jointed_bodies(seed=3, n=6000, n_joints=0, n_springs=2000, side=90.0)
     s.jnt_a = s.jnt_a[:0]
     got, want = run_gpu(s, 4), run_oracle(s, 4)
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
@@ -158,7 +158,7 @@ def test_multi_collider_bodies_bit_exact():
 
 
 def test_circle_constraint_bit_exact():
-    s = scenes.config1(seed=12, n=400)
+    s = scenes.sparse_spheres(seed=12, n=400)
     s.world_box = None
     s.circles = np.array([[0.0, 0.0, 12.0]], np.float32)
     got, want = run_gpu(s, 30), run_oracle(s, 30)
@@ -166,7 +166,7 @@ def test_circle_constraint_bit_exact():
 
 
 def test_collisions_disabled_bit_exact():
-    s = scenes.config1(seed=13, n=300)
+    s = scenes.sparse_spheres(seed=13, n=300)
     s.collisions_enabled = False
     got, want = run_gpu(s, 10), run_oracle(s, 10)
     assert_exact(got, want)
@@ -199,7 +199,7 @@ def test_config3_scaled_tolerance():
     this overlapping start (its own f32 run deviates from f64 by up to ~0.5),
     so 97% of components within 1e-4 (1 + |x|) and the largest deviation
     within 1% of the f32 reference's own."""
-    s = scenes.config3(seed=3, n=6000, n_joints=1500, n_springs=3000, side=90.0)
+    s = scenes.jointed_bodies(seed=3, n=6000, n_joints=1500, n_springs=3000, side=90.0)
     got = run_gpu(s, 1)
     ref32 = run_oracle(s, 1, precision=32, joint_order=got["joint_order"])
     err = np.abs(got["pos"].astype(np.float64) - ref32["pos"])
@@ -214,7 +214,7 @@ def test_config3_scaled_tolerance():
 # ---- batched worlds -----------------------------------------------------------
 
 def test_batched_worlds_bit_exact_per_world():
-    s = scenes.config4(seed=14, n_worlds=24, nmin=64, nmax=1024)
+    s = scenes.uneven_batch(seed=14, n_worlds=24, nmin=64, nmax=1024)
     got = run_gpu(s, 5)
     for w in range(s.n_worlds):
         sub = scenes.unpack_world(s, w)
@@ -233,7 +233,7 @@ def test_pushout_coincident_spheres_gpu():
 
 
 def test_old_dt_ratio_changes_with_dt():
-    s = scenes.config1(seed=15, n=200)
+    s = scenes.sparse_spheres(seed=15, n=200)
     with native.World(s) as w:
         w.step(1 / 60)
         w.step(1 / 60)
@@ -266,7 +266,7 @@ def test_body_collider_transform_gpu():
 
 
 def test_fixed_step_accumulator():
-    s = scenes.config1(seed=16, n=100)
+    s = scenes.sparse_spheres(seed=16, n=100)
     with native.World(s) as w:
         w.fixed_step(0.05)        # 3 steps of 1/60 (max 3), accumulator 0
         t, acc = w.time()

@@ -9,7 +9,7 @@ bit-exact -- tests/test_parity_gpu.py; this is the f64 comparison.)
 
 Tolerances, from the f32 oracle's own distance to the f64 oracle on the
 same scenes (its statistics are the GPU's):
-  config1 (1,000 spheres, 600 steps, every 50): potential energy within 1%,
+  sparse_spheres (1,000 spheres, 600 steps, every 50): potential energy within 1%,
     kinetic energy within 5% of the run's peak, cumulative contacts within
     5% + 200, penetrations: count within 30% + 20, largest within 0.02;
   dense (3,000 spheres at 40% packing with overlaps, 120 steps, every 10):
@@ -56,7 +56,7 @@ def series(scene, steps, every):
 
 
 def test_config1_rollout_statistics_match_f64():
-    s = scenes.config1(seed=1, n=1000)
+    s = scenes.sparse_spheres(seed=1, n=1000)
     g, r = series(s, 600, 50)
     ke_peak = np.abs(r[:, 0]).max()
     assert np.all(np.abs(g[:, 1] - r[:, 1]) <= 0.01 * np.abs(r[:, 1])), (g[:, 1], r[:, 1])
@@ -67,7 +67,7 @@ def test_config1_rollout_statistics_match_f64():
 
 
 def test_dense_rollout_statistics_match_f64():
-    s = scenes.config2(seed=2, n=3000)
+    s = scenes.dense_spheres(seed=2, n=3000)
     g, r = series(s, 120, 10)
     pe_big = np.abs(r[:, 1]).max()
     assert np.all(np.abs(g[:, 1] - r[:, 1]) <= 0.12 * np.abs(r[:, 1]) + 0.02 * pe_big), (g[:, 1], r[:, 1])

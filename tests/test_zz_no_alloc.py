@@ -37,7 +37,7 @@ def test_noalloc_contact_pairs_match_allocating_entry_point_twice():
     torch = pytest.importorskip("torch")
     fn, max_n = _bind()
     # multi-collider bodies with offsets and mixed groups exercise every filter
-    s = scenes.config3(seed=81, n=6000, n_joints=0, n_springs=0, side=70.0)
+    s = scenes.jointed_bodies(seed=81, n=6000, n_joints=0, n_springs=0, side=70.0)
     rng = np.random.Generator(np.random.PCG64(81))
     s.col_memb = rng.choice(np.array([1, 2, 0xFFFFFFFF], np.uint32), s.n_colliders)
     s.col_filt = rng.choice(np.array([1, 3, 0xFFFFFFFF], np.uint32), s.n_colliders)
