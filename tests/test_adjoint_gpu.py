@@ -124,7 +124,7 @@ def _check_replay(worst, fin):
     assert worst["vel"] < 2e-4 * scale, worst
 
 
-def test_config5_worlds_short_horizon_match_replay():
+def test_gradient_batch_short_horizon_matches_replay():
     """The differentiable-rollout batch at full size -- 256 worlds x 2,048
     spheres (r ~ U[0.1, 0.2], 30% packing, overlaps allowed at t = 0), 1,024
     springs per world, 64 marked bodies per world -- over 10 steps with a

@@ -48,14 +48,14 @@ def assert_exact(got, want, keys=("pos", "pos_old", "vel")):
 
 # ---- 1,000 spheres in a walled box ---------------------------------------------
 
-def test_config1_single_step_bit_exact():
+def test_sparse_single_step_bit_exact():
     s = scenes.sparse_spheres()
     got, want = run_gpu(s, 1), run_oracle(s, 1)
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
     assert got["contacts"] == want["contacts"]
 
 
-def test_config1_full_600_step_rollout_bit_exact():
+def test_sparse_full_600_step_rollout_bit_exact():
     """All 600 steps (4,800 substeps): a single differing bit anywhere would
     grow chaotically, so equality at the end pins every substep."""
     s = scenes.sparse_spheres()
@@ -85,7 +85,7 @@ def test_determinism_two_runs_bitwise_equal():
 # ---- dense overlapping spheres (scaled down) --------------------------------
 
 @pytest.mark.parametrize("n", [4096, 30000])
-def test_config2_scaled_bit_exact(n):
+def test_dense_scaled_bit_exact(n):
     s = scenes.dense_spheres(seed=2, n=n)
     got, want = run_gpu(s, 3), run_oracle(s, 3)
     assert want["pushouts"] == 0
@@ -93,7 +93,7 @@ def test_config2_scaled_bit_exact(n):
     assert got["contacts"] == want["contacts"]
 
 
-def test_config1_f64_tolerance():
+def test_sparse_f64_tolerance():
     """Sparse non-overlapping world: one step within |dx| <= 1e-4 (1 + |x|) of
     the f64 re-run, every component."""
     s = scenes.sparse_spheres(seed=21)
@@ -102,7 +102,7 @@ def test_config1_f64_tolerance():
     assert np.all(err <= 1e-4 * (1.0 + np.abs(want["pos"]))), err.max()
 
 
-def test_config2_f64_tolerance():
+def test_dense_f64_tolerance():
     """Dense overlapping start (40% packing): the reference algorithm itself
     amplifies f32 rounding at contact-threshold flips (its f32 run deviates
     from f64 by up to ~1e-2 after 8 substeps, median ~1e-6).  Stated
@@ -190,7 +190,7 @@ def test_joints_single_collider_positions_exact_in_gpu_order():
     np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
 
 
-def test_config3_scaled_tolerance():
+def test_jointed_scaled_tolerance():
     """Multi-collider bodies + joints + springs: rotation enters the snapshots
     through sin/cos and the joints through atan2 (CUDA's, not glibc's), so
     one step is compared with tolerances.  Against the oracle run in the GPU's
@@ -274,3 +274,63 @@ def test_fixed_step_accumulator():
     assert abs(t - 3 / 60) < 1e-12 and abs(acc - (0.05 - 3 / 60)) < 1e-12
     want = run_oracle(s, 3, dt=1 / 60)
     assert_exact(got, want)
+
+
+# ---- degenerate and extreme inputs ------------------------------------------
+def check_against_oracle(scene, dt, steps):
+    got = run_gpu(scene, steps, dt)
+    want = run_oracle(scene, steps, dt)
+    assert_exact(got, want)
+    assert got["contacts"] == want["contacts"]
+
+
+def test_empty_world_steps():
+    s = scenes.spheres(np.zeros((0, 2), np.float32), np.zeros(0, np.float32))
+    with native.World(s) as w:
+        w.step(1.0 / 60.0)
+        w.rollout(1.0 / 60.0, 3)
+        b = w.read_bodies()
+        assert b["pos"].shape == (0, 2)
+        assert w.contact_count() == (0, 0)
+
+
+def test_single_body_falls_like_the_oracle():
+    s = scenes.spheres(np.array([[0.5, 3.0]], np.float32), np.array([0.2], np.float32),
+                       np.array([[0.3, 0.0]], np.float32))
+    check_against_oracle(s, 1.0 / 60.0, 30)
+
+
+def test_batch_with_empty_and_single_body_worlds():
+    rng = np.random.Generator(np.random.PCG64(71))
+    empty = scenes.spheres(np.zeros((0, 2), np.float32), np.zeros(0, np.float32), box=(-5, -5, 5, 5))
+    one = scenes.spheres(np.array([[0.0, 1.0]], np.float32), np.array([0.3], np.float32),
+                         np.array([[1.0, 0.5]], np.float32), box=(-5, -5, 5, 5))
+    worlds = [scenes.random_world(rng, 200, 0.1, 0.3, 0.35, 1.0), empty, one,
+              scenes.random_world(rng, 90, 0.1, 0.3, 0.35, 1.0), empty]
+    s = scenes.pack(worlds)
+    s.dt = 1.0 / 60.0
+    with native.World(s) as w:
+        for _ in range(12):
+            w.step(s.dt)
+        got = w.read_bodies()
+    for i in range(s.n_worlds):
+        sub = scenes.unpack_world(s, i)
+        b0 = int(s.world_body_offsets[i])
+        o = oracle.OracleWorld(sub, 32)
+        assert o.step(s.dt, 12) == 0
+        want = o.bodies()
+        for k in ("pos", "pos_old", "vel"):
+            assert np.array_equal(got[k][b0:b0 + sub.n_bodies].astype(np.float64), want[k]), (i, k)
+
+
+def test_far_apart_clusters_share_a_wrapped_grid():
+    """Two clusters 1e5 apart: the grid extent is capped, so the torus wraps
+    and far cells alias; the exact test keeps the result exact."""
+    rng = np.random.Generator(np.random.PCG64(72))
+    a = rng.uniform(-3, 3, (300, 2)).astype(np.float32)
+    b = (rng.uniform(-3, 3, (300, 2)) + np.array([1e5, -7e4])).astype(np.float32)
+    pos = np.concatenate([a, b])
+    rad = rng.uniform(0.1, 0.3, 600).astype(np.float32)
+    vel = rng.normal(0, 1, (600, 2)).astype(np.float32)
+    s = scenes.spheres(pos, rad, vel)
+    check_against_oracle(s, 1.0 / 60.0, 10)

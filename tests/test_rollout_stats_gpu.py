@@ -55,7 +55,7 @@ def series(scene, steps, every):
     return np.array(gpu, float), np.array(ref, float)
 
 
-def test_config1_rollout_statistics_match_f64():
+def test_sparse_rollout_statistics_match_f64():
     s = scenes.sparse_spheres(seed=1, n=1000)
     g, r = series(s, 600, 50)
     ke_peak = np.abs(r[:, 0]).max()
