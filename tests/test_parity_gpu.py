@@ -133,10 +133,15 @@ def test_springs_bit_exact():
     assert_exact(got, want)
 
 
-def test_static_bodies_sensors_groups_bit_exact():
+def test_static_kinematic_bodies_sensors_groups_bit_exact():
     s = scenes.dense_spheres(seed=31, n=5000)
     rng = np.random.Generator(np.random.PCG64(31))
     s.body_type[rng.random(s.n_bodies) < 0.1] = scenes.STATIC
+    # kinematic bodies integrate like dynamic ones: the reference only ever
+    # tests is_static (rigid_body.rs:221-242, physics.rs:327)
+    kin = rng.random(s.n_bodies) < 0.05
+    s.body_type[kin & (s.body_type != scenes.STATIC)] = 2
+    s.body_type[(rng.random(s.n_bodies) < 0.05) & (s.body_type == 0)] = 3
     s.col_sensor[rng.random(s.n_colliders) < 0.05] = 1
     s.col_memb = rng.choice(np.array([1, 2, 3, 0xFFFFFFFF], np.uint32), s.n_colliders)
     s.col_filt = rng.choice(np.array([1, 2, 0xFFFFFFFF], np.uint32), s.n_colliders)
