@@ -6,7 +6,9 @@ packing with overlaps, walled box, seeded synthetic scene).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 One JSON line on rank 0.  `value` is device-timed (CUDA events on the
-world's stream, L2 flushed between steps, inputs resident in HBM); `e2e` is
+world's stream, L2 flushed between steps, inputs resident in HBM) over steps
+W .. W+K-1 of the scene; the phase-timing and end-to-end legs reload the
+scene and time the same window.  `e2e` is
 the same metric through the C ABI with the body state written from and read
 back into pinned host memory every step; `roofline` is the dominant kernel's
 algorithmic bytes per launch over its event-timed duration; `cpu_baseline`
@@ -67,14 +69,20 @@ class Clocks:
         self.index = index
         self.proc = None
         self.path = None
+        self.skip = 0
 
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler is running
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.skip = sum(1 for _ in open(self.path))
         except Exception:
             self.proc = None
 
@@ -88,7 +96,11 @@ class Clocks:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        lines = list(open(self.path))
+        # samples taken inside the timed region (the ones before it are dropped,
+        # unless the region was shorter than the sampling interval)
+        lines = lines[self.skip:] or lines[-1:]
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -164,7 +176,8 @@ def run_reference(args):
     import numpy as np
     from blobs_gb300 import scenes
     from oracle import oracle
-    sizes = [2048, 4096, 8192, 16384]
+    # bounded samples: the whole --steps K run stays within a few minutes
+    sizes = [2048, 4096, 8192, 16384] if args.steps <= 30 else [2048, 4096, 8192]
     ns, ts = [], []
     for i in range(args.warmup + args.steps):
         n = sizes[i % len(sizes)]
@@ -371,6 +384,14 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def restart():
+        # every leg runs the same window of the scene: steps W .. W+K-1
+        # (the scene's contact load changes along a rollout)
+        world.load(scene)
+        for _ in range(args.warmup):
+            world.step(dt)
+        barrier()
+
     for _ in range(args.warmup):
         world.step(dt)
     barrier()
@@ -394,9 +415,11 @@ def run_ours(args):
     total_ms = max_over_ranks(sum(step_ms), dist, dev)
     value = job_throughput(scene.n_bodies, args.steps, world_size, total_ms)
 
+    contacts_total, contacts_last = world.contact_count()
+
     # -- per-phase kernel time (events captured into the step graph) ---------
     world.set_timing(True)
-    world.step(dt)  # capture the instrumented graph
+    restart()  # the instrumented graph is captured during the warm-up
     world.phase_times()
     phase = {p: [0.0, 0] for p in native.World.PHASES}
     for i in range(args.steps):
@@ -417,6 +440,7 @@ def run_ours(args):
     h_pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
     h_old = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
     h_vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+    restart()
     world.read_bodies_into(h_pos, h_old, h_vel)
     e2e_s = []
     for i in range(args.steps):
@@ -428,7 +452,6 @@ def run_ours(args):
         world.read_bodies_into(h_pos, h_old, h_vel)   # synchronising
         e2e_s.append(time.perf_counter() - t0)
     e2e_value = job_throughput(n, args.steps, world_size, 1e3 * max_over_ranks(sum(e2e_s), dist, dev))
-    contacts_total, contacts_last = world.contact_count()
     world.sync()
 
     whole_achieved = BYTES_PER_BODY_SUBSTEP * scene.substeps * value / 1e9 / world_size
@@ -441,7 +464,9 @@ def run_ours(args):
                                "dt=1/120, 8 substeps/step" % (float(scene.world_box[0, 2] * 2)),
                    "bodies": scene.n_bodies, "substeps": scene.substeps, "parallelism": "replicas" if world_size > 1
                    else "single", "l2": "flushed (256 MiB write) before every timed step",
-                   "contacts_last_substep": contacts_last, "cell_scale": cell_scale},
+                   "contacts_last_substep": contacts_last, "cell_scale": cell_scale,
+                   "window": "steps %d-%d of the scene; the phase-timing and end-to-end legs reload the scene and "
+                             "run the same window" % (args.warmup, args.warmup + args.steps - 1)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": dom_ms,
@@ -473,7 +498,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
