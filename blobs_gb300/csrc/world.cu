@@ -148,6 +148,7 @@ struct blobs_world {
     uint32_t n_steps = 0, every = 0, n_seg = 0;
     float old_dt0 = 1.0f;
     bool pending0 = false;
+    uint32_t substeps = 0;
     float2* ckpt = nullptr;  // (n_seg + 1) x 4 x n_bodies float2: p, po, s, v
   } rec;
   // collision event stream (physics.rs:304-311), off unless enabled
@@ -195,10 +196,14 @@ struct blobs_world {
     eager_timing.destroy();
     launched_sets.clear();
   }
-  void release() {
-    drop_graphs();
+  // the recorded rollout (checkpoints sized for the loaded scene) is dropped
+  void drop_recording() {
     if (rec.ckpt) cudaFree(rec.ckpt);
     rec = Recording();
+  }
+  void release() {
+    drop_graphs();
+    drop_recording();
     if (ev_mem) cudaFree(ev_mem);
     ev_mem = nullptr;
     events_on = false;
@@ -972,6 +977,7 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   if (st) return st;
   cudaStreamSynchronize(w->st());
   w->drop_graphs();
+  w->drop_recording();
   if (w->arena) cudaFree(w->arena);
   w->arena = nullptr;
   w->loaded = false;
@@ -1385,6 +1391,7 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
   r.n_seg = n_seg;
   r.old_dt0 = w->old_dt;
   r.pending0 = w->pending;
+  r.substeps = w->cfg.substeps;
   for (uint32_t g = 0; g <= n_seg; ++g) {
     float2* base = r.ckpt + 4 * nb * g;
     gather_state(w, base, base + nb, base + 2 * nb, base + 3 * nb);
@@ -1401,7 +1408,7 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
 
 int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
-  if (!w->loaded || !w->rec.valid) return BLOBS_ERR_STATE;
+  if (!w->loaded || !w->rec.valid || w->rec.substeps != w->cfg.substeps) return BLOBS_ERR_STATE;
   if (!dl_dpos) return BLOBS_ERR_INVALID_ARGUMENT;
   cudaSetDevice(w->cfg.device);
   auto& r = w->rec;
@@ -1559,6 +1566,7 @@ int blobs_world_set_events(blobs_world* w, int enabled, uint32_t capacity) {
   if (e != cudaSuccess) return blobs_map_cuda(e);
   const bool was_on = w->events_on;
   w->drop_graphs();  // the event pointers and the fusion choice are baked into graphs
+  w->drop_recording();  // checkpoints hold V in the previous mode
   if (w->ev_mem) cudaFree(w->ev_mem);
   w->ev_mem = nullptr;
   w->ev_host.clear();

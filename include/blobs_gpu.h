@@ -247,7 +247,9 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
  * forward pass) with its contacts recorded, then reversed substep by
  * substep.  Contacts resolved by the push-out branch (coincident centres,
  * physics.rs:272-286) are not differentiated.  The world is left in the
- * rollout's final state.  Allocates its scratch per call: 24 B per body per
+ * rollout's final state.  A reload, a change of the substep count or of the
+ * event mode drops the recording (then BLOBS_ERR_STATE).  Allocates its
+ * scratch per call: 24 B per body per
  * recorded substep state plus 8 B x (4 n_bodies + 1024) per substep of one
  * checkpoint segment.  The derivative of long contact-rich rollouts can
  * exceed the f32 range; such gradients come back as +-inf or NaN with

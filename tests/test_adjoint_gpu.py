@@ -243,6 +243,26 @@ def test_backward_without_record_is_a_state_error():
         assert ei.value.status == native.ERR_STATE
 
 
+def test_reload_or_substep_change_drops_the_recording():
+    scene, _, _ = make_scene(seed=8, n_worlds=1)
+    small, _, _ = make_scene(seed=9, n_worlds=1, n=40)
+    g = np.zeros((scene.n_bodies, 2), np.float32)
+    with native.World(scene) as w:
+        w.rollout_record(scene.dt, 3, 2)
+        w.load(small)  # checkpoints of the old scene must not be restored
+        with pytest.raises(native.BlobsError) as ei:
+            w.backward(np.zeros((small.n_bodies, 2), np.float32), small.n_springs)
+        assert ei.value.status == native.ERR_STATE
+        w.load(scene)
+        w.rollout_record(scene.dt, 3, 2)
+        cfg = native.make_config(scene)
+        cfg.substeps = 4
+        native.check(native.lib().blobs_world_set_config(w._h, native.ctypes.byref(cfg)), "set_config")
+        with pytest.raises(native.BlobsError) as ei:
+            w.backward(g, scene.n_springs)
+        assert ei.value.status == native.ERR_STATE
+
+
 @pytest.mark.parametrize("n_worlds", [1, 2])
 def test_recorded_rollout_equals_plain_steps(n_worlds):
     """The checkpointed forward pass is the ordinary step, bit for bit, and a
