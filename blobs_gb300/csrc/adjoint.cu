@@ -15,11 +15,16 @@
 //
 // Three kernels per substep, in order:
 //   k_adj_body    per body: Verlet, clamp mask, velocity request -> the
-//                 adjoints of p_c and a, the outgoing adjoints of p and po
-//   k_adj_pairs   per recorded contact: the Jacobian of the mass-ratio
-//                 correction -> adjoints of both snapshots
+//                 adjoints of p_c and a, the outgoing adjoint of po
 //   k_adj_springs per spring: Jacobians of the (quirky) spring force ->
-//                 adjoints of both positions and velocities, and dL/dk
+//                 the adjoints of the spring's d = pb - pa and rv = va - vb,
+//                 and dL/dk
+//   k_adj_gather  per body: its recorded contacts (the Jacobian of the
+//                 mass-ratio correction, each pair evaluated from both
+//                 sides) -> the adjoint of its snapshot; its springs ->
+//                 the adjoints of its position and velocity
+// Every sum runs in a fixed order (ascending partner id, ascending spring
+// index), so the gradients are deterministic: no float atomics.
 #include "device.cuh"
 #include "kernels.h"
 
@@ -62,44 +67,13 @@ __global__ void __launch_bounds__(256) k_adj_body(WorldDev w, AdjointSubstep a) 
   }
   a.lpc[b] = lpc;
   a.la[b] = la;
-  a.lp_out[b] = lpc;  // p_c = p + corrections(s)
   a.lpo_out[b] = lpo;
-  a.ls_out[b] = v2(0.0f, 0.0f);
-  a.lv_out[b] = v2(0.0f, 0.0f);
-}
-
-__global__ void __launch_bounds__(256) k_adj_pairs(WorldDev w, AdjointSubstep a) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t n = min(*a.n_pairs, a.pair_cap);
-  if (k >= n) return;
-  const uint2 pr = a.pairs[k];
-  if (pr.y & 0x80000000u) return;  // push-out: not differentiated
-  const uint32_t ia = pr.x, ib = pr.y;
-  if (ia >= w.n_bodies || ib >= w.n_bodies) return;
-  const float2 sa = a.s_t[ia], sb = a.s_t[ib];
-  const float ax = sa.x - sb.x, ay = sa.y - sb.y;
-  const float d = sqrtf(ax * ax + ay * ay);
-  if (!(d > 0.0f)) return;
-  const float nx = ax / d, ny = ay / d;
-  const float R = w.col_radius[ia] + w.col_radius[ib];
-  const float ma = w.mass[ia], mb = w.mass[ib];
-  const float rho = 1.0f - ma / (ma + mb);
-  // corr_a = rho * delta * n, corr_b = -(1 - rho) * delta * n with delta n = R axis / d - axis;
-  // d(delta n)/d axis = J = (R/d)(I - n n^T) - I, symmetric
-  const float2 la_ = a.lpc[ia], lb_ = a.lpc[ib];
-  const float ux = rho * la_.x - (1.0f - rho) * lb_.x, uy = rho * la_.y - (1.0f - rho) * lb_.y;
-  const float q = R / d;
-  const float jxx = q * (1.0f - nx * nx) - 1.0f, jyy = q * (1.0f - ny * ny) - 1.0f, jxy = -q * nx * ny;
-  const float gx = jxx * ux + jxy * uy, gy = jxy * ux + jyy * uy;
-  atomicAdd(&a.ls_out[ia].x, gx);
-  atomicAdd(&a.ls_out[ia].y, gy);
-  atomicAdd(&a.ls_out[ib].x, -gx);
-  atomicAdd(&a.ls_out[ib].y, -gy);
 }
 
 __global__ void __launch_bounds__(256) k_adj_springs(WorldDev w, AdjointSubstep a) {
   const uint32_t sidx = blockIdx.x * blockDim.x + threadIdx.x;
   if (sidx >= w.n_springs) return;
+  a.spr_terms[sidx] = make_float4(0.f, 0.f, 0.f, 0.f);
   const uint32_t ia = w.spr_a[sidx], ib = w.spr_b[sidx];
   const bool sa_static = (w.bflags[ia] & BF_STATIC) != 0, sb_static = (w.bflags[ib] & BF_STATIC) != 0;
   // force adjoint: a_a += F / m_a, a_b += -F / m_b (static bodies take no force)
@@ -140,21 +114,71 @@ __global__ void __launch_bounds__(256) k_adj_springs(WorldDev w, AdjointSubstep 
   const float lrvy = -c * (ex * ex * ey * mux + ey * ey * ey * muy);
   // dF_i/dk = (dist - L) e_i
   a.lk[sidx] += (dist - L) * (ex * mux + ey * muy);
-  atomicAdd(&a.lp_out[ib].x, ldx);
-  atomicAdd(&a.lp_out[ib].y, ldy);
-  atomicAdd(&a.lp_out[ia].x, -ldx);
-  atomicAdd(&a.lp_out[ia].y, -ldy);
-  atomicAdd(&a.lv_out[ia].x, lrvx);
-  atomicAdd(&a.lv_out[ia].y, lrvy);
-  atomicAdd(&a.lv_out[ib].x, -lrvx);
-  atomicAdd(&a.lv_out[ib].y, -lrvy);
+  // d = pb - pa, rv = va - vb: k_adj_gather adds +-these at both ends
+  a.spr_terms[sidx] = make_float4(ldx, ldy, lrvx, lrvy);
+}
+
+__global__ void __launch_bounds__(256) k_adj_gather(WorldDev w, AdjointSubstep a) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= w.n_bodies) return;
+  // contacts: p_c(hi) += rho d(n) ... on s_hi - s_lo, evaluated from this body's side
+  float2 ls = v2(0.0f, 0.0f);
+  const uint32_t nrec = min(a.rec_n[c], REC_CAP);
+  const float2 sc = a.s_t[c];
+  const float rc = w.col_radius[c], mc = w.mass[c];
+  for (uint32_t e = 0; e < nrec; ++e) {
+    const uint32_t rec = a.rec_list[(size_t)e * w.n_bodies + c];
+    if (rec & 0x80000000u) continue;  // push-out: not differentiated
+    const uint32_t o = rec;
+    if (o >= w.n_bodies || o == c) continue;
+    const bool hi = c > o;
+    const uint32_t ia = hi ? c : o, ib = hi ? o : c;
+    const float2 so = a.s_t[o];
+    const float2 sa = hi ? sc : so, sb = hi ? so : sc;
+    const float ax = sa.x - sb.x, ay = sa.y - sb.y;
+    const float d = sqrtf(ax * ax + ay * ay);
+    if (!(d > 0.0f)) continue;
+    const float nx = ax / d, ny = ay / d;
+    const float R = rc + w.col_radius[o];
+    const float mo = w.mass[o];
+    const float ma = hi ? mc : mo, mb = hi ? mo : mc;
+    const float rho = 1.0f - ma / (ma + mb);
+    // corr_a = rho * delta * n, corr_b = -(1 - rho) * delta * n with
+    // delta n = R axis / d - axis; d(delta n)/d axis = J = (R/d)(I - n n^T) - I, symmetric
+    const float2 la_ = a.lpc[ia], lb_ = a.lpc[ib];
+    const float ux = rho * la_.x - (1.0f - rho) * lb_.x, uy = rho * la_.y - (1.0f - rho) * lb_.y;
+    const float q = R / d;
+    const float jxx = q * (1.0f - nx * nx) - 1.0f, jyy = q * (1.0f - ny * ny) - 1.0f, jxy = -q * nx * ny;
+    const float gx = jxx * ux + jxy * uy, gy = jxy * ux + jyy * uy;
+    ls = hi ? v2(ls.x + gx, ls.y + gy) : v2(ls.x - gx, ls.y - gy);
+  }
+  a.ls_out[c] = ls;
+  // springs, ascending spring index: p_c = p + corrections(s), so the
+  // position adjoint is lpc plus the spring terms
+  float2 lp = a.lpc[c], lv = v2(0.0f, 0.0f);
+  if (w.n_springs) {
+    const uint32_t q0 = w.body_spr_start[c], q1 = w.body_spr_start[c + 1];
+    for (uint32_t qq = q0; qq < q1; ++qq) {
+      const uint32_t e = w.body_spr[qq];
+      const float4 t = a.spr_terms[e >> 1];
+      if (e & 1u) {  // endpoint b: +d, -rv
+        lp = v2(lp.x + t.x, lp.y + t.y);
+        lv = v2(lv.x - t.z, lv.y - t.w);
+      } else {       // endpoint a: -d, +rv
+        lp = v2(lp.x - t.x, lp.y - t.y);
+        lv = v2(lv.x + t.z, lv.y + t.w);
+      }
+    }
+  }
+  a.lp_out[c] = lp;
+  a.lv_out[c] = lv;
 }
 
 void launch_adjoint_substep(const WorldDev& w, const AdjointSubstep& a, cudaStream_t st) {
   if (!w.n_bodies) return;
   k_adj_body<<<(w.n_bodies + 255u) / 256u, 256, 0, st>>>(w, a);
-  if (a.pair_cap) k_adj_pairs<<<(a.pair_cap + 255u) / 256u, 256, 0, st>>>(w, a);
   if (w.n_springs) k_adj_springs<<<(w.n_springs + 255u) / 256u, 256, 0, st>>>(w, a);
+  k_adj_gather<<<(w.n_bodies + 255u) / 256u, 256, 0, st>>>(w, a);
 }
 
 }  // namespace blobs

@@ -206,11 +206,14 @@ struct SingleArgs {
   float dt, ratio_first, ratio_rest;
   uint32_t contacts, pending, springs, rot_dynamic, do_keys, write_v, move_v;
   uint32_t v_vel;            // V holds calculated_velocity (else the displacement of the last substep)
-  // contact recording for the adjoint (NULL in ordinary steps): pairs
-  // (hi, lo | pushed << 31) in arena ids
-  uint2* rec_pairs;
-  uint32_t* rec_count;
-  uint32_t rec_cap;
+  // contact recording for the adjoint (NULL in ordinary steps): every
+  // contact of body c in the order it was applied (ascending partner id),
+  // rec_list[k * n_bodies + c] = partner | pushed << 31 for k < REC_CAP,
+  // rec_n[c] = the number of contacts (more than REC_CAP: overflow),
+  // *rec_max = the largest rec_n of the substep
+  uint32_t* rec_list;
+  uint32_t* rec_n;
+  uint32_t* rec_max;
 };
 
 // Append one collision event (physics.rs:304-311): the pair (a, b) with
@@ -229,5 +232,6 @@ constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
 constexpr uint32_t COUNTER_BINS = 64;
+constexpr uint32_t REC_CAP = 16;           // recorded contacts per body and substep (adjoint)
 
 }  // namespace blobs

@@ -41,8 +41,8 @@ struct AdjointSubstep {
   const float2* v_t;
   const float2* p_t1;
   const float2* s_t1;
-  const uint2* pairs;      // contacts resolved in the substep (hi, lo | pushed << 31)
-  const uint32_t* n_pairs;
+  const uint32_t* rec_list;  // contacts of each body in the substep, as recorded (REC_CAP x n_bodies)
+  const uint32_t* rec_n;     // per body: recorded contacts
   // adjoints of the state after the substep (in) and before it (out)
   const float2* lp_in;
   const float2* lpo_in;
@@ -56,11 +56,11 @@ struct AdjointSubstep {
   float2* la;              // scratch: adjoint of the acceleration
   float2* lv0;             // gradient of the velocity requests (first substep of the rollout)
   float* lk;               // gradient of the spring stiffnesses (accumulated)
+  float4* spr_terms;       // scratch: per spring, the adjoint of d (pb - pa) and of rv (va - vb)
   float dt;
   float ratio_first;       // dt / old_dt for the first dynamic body (first substep only)
   uint32_t first_substep;  // the rollout's first substep (dt / old_dt applies)
   uint32_t vreq_pending;   // velocity requests were pending at the rollout's start
-  uint32_t pair_cap;
 };
 void launch_adjoint_substep(const WorldDev& w, const AdjointSubstep& a, cudaStream_t st);
 

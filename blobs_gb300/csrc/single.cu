@@ -153,10 +153,12 @@ __device__ __forceinline__ bool single_pair(const WorldDev& w, const SingleArgs&
   return true;
 }
 
-// Append a resolved contact (arena ids, hi > lo) for the adjoint pass.
-__device__ __forceinline__ void record_pair(const SingleArgs& a, uint32_t hi, uint32_t lo, bool pushed) {
-  const uint32_t k = atomicAdd(a.rec_count, 1u);
-  if (k < a.rec_cap) a.rec_pairs[k] = make_uint2(hi, lo | (pushed ? 0x80000000u : 0u));
+// Record a contact of body c (its partner, in the order applied) for the
+// adjoint pass.
+__device__ __forceinline__ void record_contact(const WorldDev& w, const SingleArgs& a, uint32_t c, uint32_t other,
+                                               bool pushed, uint32_t& nrec) {
+  if (nrec < REC_CAP) a.rec_list[(size_t)nrec * w.n_bodies + c] = other | (pushed ? 0x80000000u : 0u);
+  ++nrec;
 }
 
 // Collision event of the pair (c, lo), c > lo: velocities from the V buffer
@@ -222,7 +224,8 @@ __device__ __forceinline__ BodyConst body_const(const WorldDev& w, const WorldPa
 // arena id (many candidates, or any layout): O(contacts x candidates).
 template <int MODE>
 __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Segments& g, uint32_t j, uint32_t c,
-                                float2 p0, float2 s, float r, float m, uint32_t& ncontacts, uint32_t& npush) {
+                                float2 p0, float2 s, float r, float m, uint32_t& ncontacts, uint32_t& npush,
+                                uint32_t& nrec) {
   const float4* __restrict__ C = a.cand;
   float2 p = p0;
   uint32_t last = 0u;
@@ -250,10 +253,10 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
     single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp);
     if (sp.pushed) p = add(p, sp.push);
     p = add(p, sp.corr);
+    if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
     if (best < c) {
       ++ncontacts;
       npush += sp.pushed ? 1u : 0u;
-      if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
       if (w.ev_rec) single_event(w, a, c, j, best);
     }
     last = best;
@@ -315,6 +318,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
     const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
     const float2 p0 = v2(bv.x, bv.y);  // position at the start of the substep
     float2 p = p0;
+    uint32_t nrec = 0;  // contacts recorded for the adjoint
 
     const uint32_t own_key = a.contacts ? a.own_cell[j] : 0u;
     const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
@@ -368,15 +372,15 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
           p = add(p, sp.corr);
+          if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
-            if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
             if (w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
-        p = contacts_walk<MODE>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush);
+        p = contacts_walk<MODE>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
       }
     } else if (a.contacts) {
       // cells on the grid edge (the torus wraps): general segments
@@ -419,16 +423,21 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
           p = add(p, sp.corr);
+          if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
-            if (a.rec_pairs) record_pair(a, c, best, sp.pushed);
             if (w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
-        p = contacts_walk<MODE>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush);
+        p = contacts_walk<MODE>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
       }
+    }
+
+    if (a.rec_list) {
+      a.rec_n[c] = nrec;
+      if (nrec) atomicMax(a.rec_max, nrec);
     }
 
     // ---- update_objects (physics.rs:323-367) with gravity + springs ----

@@ -138,9 +138,9 @@ struct blobs_world {
   bool timing = false;
   float cell_scale = 1.0f;             // cell edge = scale x the smallest exact edge (autotuned)
   // contact recording of the eager path (adjoint recomputation)
-  uint2* rec_pairs = nullptr;
-  uint32_t* rec_count = nullptr;
-  uint32_t rec_cap = 0;
+  uint32_t* rec_list = nullptr;
+  uint32_t* rec_n = nullptr;
+  uint32_t* rec_max = nullptr;
   // differentiable rollout: checkpoints of the arena-order state
   struct Recording {
     bool valid = false;
@@ -639,9 +639,9 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.write_v = last_in_step ? 1u : 0u;
     a.move_v = w->v_tracks() ? 1u : 0u;
     a.v_vel = w->v_tracks() ? 1u : 0u;
-    a.rec_pairs = w->rec_pairs;
-    a.rec_count = w->rec_count;
-    a.rec_cap = w->rec_cap;
+    a.rec_list = w->rec_list;
+    a.rec_n = w->rec_n;
+    a.rec_max = w->rec_max;
     int in = cur, out = cur ^ 1;
     if (coll) {
       if (!w->keys_valid) {
@@ -1414,14 +1414,15 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   auto& r = w->rec;
   const size_t nb = w->nb;
   const uint32_t S = r.every * w->cfg.substeps;  // substeps per full segment
-  const uint32_t cap = (uint32_t)std::min<size_t>(4 * nb + 1024, 0x7fffffffu);
   cudaStream_t st = w->st();
   // scratch of the reverse pass: sized by a first carve, then carved
   const size_t slice = nb * sizeof(float2);
   struct Scratch {
     float2 *sp, *ss, *sv, *adj[2][4], *lpc, *la, *lv0;
-    uint2* pairs;
-    uint32_t* counts;
+    uint32_t* rec_list;
+    uint32_t* rec_n;
+    uint32_t* rec_max;
+    float4* spr_terms;
     float* lk;
     Counters* saved;
   } x;
@@ -1429,8 +1430,10 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
     x.sp = cv.take<float2>(nb * (S + 1));  // p, s, v of every recorded state
     x.ss = cv.take<float2>(nb * (S + 1));
     x.sv = cv.take<float2>(nb * (S + 1));
-    x.pairs = cv.take<uint2>((size_t)cap * S);  // contacts of every substep
-    x.counts = cv.take<uint32_t>(S);
+    x.rec_list = cv.take<uint32_t>((size_t)REC_CAP * nb * S);  // contacts of every body and substep
+    x.rec_n = cv.take<uint32_t>(nb * S);
+    x.rec_max = cv.take<uint32_t>(S);
+    x.spr_terms = cv.take<float4>(w->ns ? w->ns : 1);
     for (int k = 0; k < 2; ++k)
       for (int m = 0; m < 4; ++m) x.adj[k][m] = cv.take<float2>(nb);  // adjoints of (p, po, s, v) in / out
     x.lpc = cv.take<float2>(nb);
@@ -1451,8 +1454,9 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   float2* const sp = x.sp;
   float2* const ss = x.ss;
   float2* const sv = x.sv;
-  uint2* const pairs = x.pairs;
-  uint32_t* const counts = x.counts;
+  uint32_t* const rec_list = x.rec_list;
+  uint32_t* const rec_n = x.rec_n;
+  uint32_t* const rec_max = x.rec_max;
   float2* const lpc = x.lpc;
   float2* const la = x.la;
   float2* const lv0 = x.lv0;
@@ -1469,7 +1473,7 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   // the recomputed substeps are not new collisions: no events
   w->dev.ev_rec = nullptr;
   int status = BLOBS_OK;
-  std::vector<uint32_t> hcounts(S);
+  std::vector<uint32_t> hmax(S);
   for (int g = (int)r.n_seg - 1; g >= 0 && e == cudaSuccess && status == BLOBS_OK; --g) {
     const uint32_t steps = std::min(r.every, r.n_steps - (uint32_t)g * r.every);
     const uint32_t nsub = steps * w->cfg.substeps;
@@ -1481,24 +1485,24 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
     cudaMemcpyAsync(sp, ck, slice, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(ss, ck + 2 * nb, slice, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(sv, ck + 3 * nb, slice, cudaMemcpyDeviceToDevice, st);
-    cudaMemsetAsync(counts, 0, sizeof(uint32_t) * S, st);
-    w->rec_cap = cap;
+    cudaMemsetAsync(rec_max, 0, sizeof(uint32_t) * S, st);
     for (uint32_t t = 0; t < nsub; ++t) {
-      w->rec_pairs = pairs + (size_t)cap * t;
-      w->rec_count = counts + t;
+      w->rec_list = rec_list + (size_t)REC_CAP * nb * t;
+      w->rec_n = rec_n + nb * t;
+      w->rec_max = rec_max + t;
       const uint32_t sub = t % w->cfg.substeps;
       enqueue_substep(w, dt_sub, w->old_dt, w->pending, sub == 0, sub + 1 == w->cfg.substeps);
       w->pending = false;
       if (w->any_dynamic) w->old_dt = dt_sub;
       gather_state(w, sp + nb * (t + 1), nullptr, ss + nb * (t + 1), sv + nb * (t + 1));
     }
-    w->rec_pairs = nullptr;
-    w->rec_count = nullptr;
-    w->rec_cap = 0;
-    e = cudaMemcpyAsync(hcounts.data(), counts, sizeof(uint32_t) * nsub, cudaMemcpyDeviceToHost, st);
+    w->rec_list = nullptr;
+    w->rec_n = nullptr;
+    w->rec_max = nullptr;
+    e = cudaMemcpyAsync(hmax.data(), rec_max, sizeof(uint32_t) * nsub, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     for (uint32_t t = 0; t < nsub && e == cudaSuccess; ++t)
-      if (hcounts[t] > cap) status = BLOBS_ERR_OVERFLOW;
+      if (hmax[t] > REC_CAP) status = BLOBS_ERR_OVERFLOW;  // a body with more contacts than recorded
     // reverse substeps of the segment
     for (int t = (int)nsub - 1; t >= 0 && status == BLOBS_OK; --t) {
       AdjointSubstep a;
@@ -1508,9 +1512,9 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
       a.v_t = w->has_springs ? sv + nb * t : nullptr;
       a.p_t1 = sp + nb * (t + 1);
       a.s_t1 = ss + nb * (t + 1);
-      a.pairs = pairs + (size_t)cap * t;
-      a.n_pairs = counts + t;
-      a.pair_cap = cap;
+      a.rec_list = rec_list + (size_t)REC_CAP * nb * t;
+      a.rec_n = rec_n + nb * t;
+      a.spr_terms = x.spr_terms;
       a.lp_in = adj[in][0];
       a.lpo_in = adj[in][1];
       a.ls_in = adj[in][2];

@@ -248,12 +248,13 @@ int blobs_world_rollout_record(blobs_world* w, double delta, uint32_t n_steps, u
  * substep.  Contacts resolved by the push-out branch (coincident centres,
  * physics.rs:272-286) are not differentiated.  The world is left in the
  * rollout's final state.  A reload, a change of the substep count or of the
- * event mode drops the recording (then BLOBS_ERR_STATE).  Allocates its
- * scratch per call: 24 B per body per
- * recorded substep state plus 8 B x (4 n_bodies + 1024) per substep of one
- * checkpoint segment.  The derivative of long contact-rich rollouts can
- * exceed the f32 range; such gradients come back as +-inf or NaN with
- * BLOBS_OK.  Synchronising. */
+ * event mode drops the recording (then BLOBS_ERR_STATE).  Every sum runs
+ * in a fixed order: the gradients are deterministic.  Allocates its scratch
+ * per call: 92 B per body per substep of one checkpoint segment (the state
+ * after the substep and up to 16 recorded contacts); a body with more than
+ * 16 contacts in one substep gives BLOBS_ERR_OVERFLOW.  The derivative of
+ * long contact-rich rollouts can exceed the f32 range; such gradients come
+ * back as +-inf or NaN with BLOBS_OK.  Synchronising. */
 int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, float* dl_dk);
 
 /* Autotuner (no counterpart in the reference): loads `scene` with each of a
