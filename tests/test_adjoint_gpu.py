@@ -83,14 +83,16 @@ def _close(got, want, what):
     assert not bad.any(), (what, int(bad.sum()), float(err.max()), float(scale))
 
 
-@pytest.mark.parametrize("steps,every,n_worlds,n_static,warm", [
-    (8, 3, 3, 0, 0),    # batched worlds, damped springs, walls
-    (12, 4, 1, 0, 0),   # one world
-    (6, 6, 2, 12, 0),   # static bodies, one segment
-    (5, 2, 2, 0, 1),    # velocity requests already consumed, old_dt = dt
+@pytest.mark.parametrize("steps,every,n_worlds,n_static,warm,walls", [
+    (8, 3, 3, 0, 0, True),    # batched worlds, damped springs, walls
+    (12, 4, 1, 0, 0, True),   # one world
+    (6, 6, 2, 12, 0, True),   # static bodies, one segment
+    (5, 2, 2, 0, 1, True),    # velocity requests already consumed, old_dt = dt
+    (7, 3, 2, 0, 0, False),   # no walls
 ])
-def test_gradients_match_replay_of_traced_oracle(steps, every, n_worlds, n_static, warm):
-    scene, marked, targets = make_scene(seed=steps + 10 * n_static, n_worlds=n_worlds, n_static=n_static)
+def test_gradients_match_replay_of_traced_oracle(steps, every, n_worlds, n_static, warm, walls):
+    scene, marked, targets = make_scene(seed=steps + 10 * n_static, n_worlds=n_worlds, n_static=n_static,
+                                        walls=walls)
     final, g, after, gv, gk = gpu_gradients(scene, marked, targets, steps, every, warm_steps=warm)
     # backward() leaves the world in the rollout's final state
     assert np.array_equal(final, after)

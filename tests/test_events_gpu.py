@@ -134,3 +134,24 @@ def test_drain_without_events_is_a_state_error():
         with pytest.raises(native.BlobsError) as ei:
             w.drain_events()
         assert ei.value.status == native.ERR_STATE
+
+
+def test_events_with_fixed_joints_in_gpu_order():
+    """Single-collider bodies with fixed joints take the joint path's contact
+    kernel; against the oracle run in the GPU's joint colour order the events
+    (pairs, order, impact velocities) are bit-exact."""
+    rng = np.random.Generator(np.random.PCG64(48))
+    s = scenes.random_world(rng, 1500, 0.1, 0.25, 0.25, 0.5)
+    near = scenes._pairs_within(s.pos, 1.0)
+    pick = np.sort(rng.choice(len(near), 500, replace=False))
+    scenes.add_fixed_joints(s, near[pick, 0], near[pick, 1])
+    with native.World(s) as w:
+        w.set_events(True, 1 << 20)
+        for _ in range(3):
+            w.step(s.dt)
+        got = w.drain_events()
+        order = w.joint_order()[0]
+    o = oracle.OracleWorld(s, 32, record_events=True, joint_order=order)
+    assert o.step(s.dt, 3) == 0
+    a, b, va, vb = o.events()
+    assert_same_events(got, (a, b, va.astype(np.float32), vb.astype(np.float32)))
