@@ -28,6 +28,7 @@
 //   thunderdome Arena iteration = ascending slot order (= insertion order for a
 //   world that never removed anything; the scene arrays are given in that order).
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -219,7 +220,7 @@ typedef struct oracle_scene {
   double box_hi[2];
 } oracle_scene;
 
-enum { ORACLE_OK = 0, ORACLE_INVALID = 2, ORACLE_NAN = 4 };
+enum { ORACLE_OK = 0, ORACLE_INVALID = 2, ORACLE_NAN = 4, ORACLE_GRID_PUSHOUT = 8, ORACLE_GRID_UNUSABLE = 16 };
 
 }  // extern "C"
 
@@ -280,6 +281,9 @@ class WorldBase {
   // the state at the start of every substep (position, position_old,
   // collider snapshots, calculated_velocity) and the contacts it resolved.
   bool tracing = false;
+  // Enumerate contact candidates through a uniform grid (the same pairs in
+  // the same order as the C^2/2 loop; for full-size checks).
+  bool grid_pairs = false;
   std::vector<double> trace_states;
   std::vector<uint32_t> trace_pairs;    // (i, j | push-out << 31), collider ids, i > j
   std::vector<uint64_t> trace_counts;   // contacts per substep
@@ -324,6 +328,15 @@ template <class T> class World : public WorldBase {
   bool box_enabled;
   V2<T> box_lo, box_hi;
   SpatialHash* shash = nullptr;
+  struct GridItem {
+    V2<T> snap;
+    T radius;
+    uint32_t memb, filt, parent, c;
+    uint64_t key;  // (row << 32) | column
+  };
+  std::vector<uint32_t> grid_gx, grid_gy, grid_tmp, grid_order, grid_count;
+  std::vector<GridItem> grid_items;
+  std::vector<uint64_t> grid_pairs_found;
 
   explicit World(const oracle_scene& s) {
     gravity = {(T)s.gravity[0], (T)s.gravity[1]};
@@ -431,54 +444,163 @@ template <class T> class World : public WorldBase {
     return (a.memb & b.filt) != 0 && (b.memb & a.filt) != 0;
   }
 
-  // physics.rs:241-317 (+ mass_ratio :319-321)
+  // One pair of the reference's contact loop (physics.rs:248-316): groups,
+  // same-parent skip, f32 distance test, push-out branch, position
+  // correction by mass ratio (:319-321), event.  Returns -1 if the pair is no
+  // contact, 1 if it is one whose push-out moved the two snapshots, else 0 or
+  // 2 for a status.
+  int resolve_pair(uint32_t i, uint32_t j, uint64_t& count) {
+    Collider& ca = cols[i];
+    Collider& cb = cols[j];
+    if (!groups_test(ca, cb)) return -1;
+    if (ca.parent == cb.parent) return -1;
+    V2<T> axis = ca.snap - cb.snap;
+    T distance = length(axis);
+    T min_dist = ca.radius + cb.radius;
+    if (!(distance < min_dist)) return -1;
+    Body& ra = bodies[ca.parent];
+    Body& rb = bodies[cb.parent];
+    const bool distance_pushed = distance < (T)1e-6f;
+    if (distance_pushed) {
+      V2<T> push = {(T)0.01f, (T)0};
+      ra.pos = ra.pos + push;
+      rb.pos = rb.pos - push;
+      ca.snap = ra.pos + ca.off;
+      cb.snap = rb.pos + cb.off;
+      axis = ca.snap - cb.snap;
+      distance = length(axis);
+      ++pushouts;
+    }
+    V2<T> va = ra.vcalc, vb = rb.vcalc;
+    if (!ca.sensor && !cb.sensor) {
+      V2<T> n = axis / distance;
+      if (isnan2(n)) return 2 + ORACLE_NAN;  // physics.rs:293 assert
+      T delta = min_dist - distance;
+      T ratio = (T)1 - ra.mass / (ra.mass + rb.mass);
+      ra.pos = ra.pos + (ratio * delta) * n;
+      rb.pos = rb.pos - (((T)1 - ratio) * delta) * n;
+    }
+    ++count;
+    if (tracing) {
+      trace_pairs.push_back(i);
+      trace_pairs.push_back(j | (distance_pushed ? 0x80000000u : 0u));
+    }
+    if (record_events) events.push_back(Event{i, j, {(double)va.x, (double)va.y}, {(double)vb.x, (double)vb.y}});
+    return distance_pushed ? 1 : 0;
+  }
+
+  // physics.rs:241-317: every collider pair (i, j < i) in arena order.
   int brute_force_collisions() {
     uint64_t count = 0;
     const uint32_t nc = (uint32_t)cols.size();
-    for (uint32_t i = 0; i < nc; ++i) {
-      for (uint32_t j = 0; j < i; ++j) {
-        Collider& ca = cols[i];
-        Collider& cb = cols[j];
-        if (!groups_test(ca, cb)) continue;
-        if (ca.parent == cb.parent) continue;
-        V2<T> axis = ca.snap - cb.snap;
-        T distance = length(axis);
-        T min_dist = ca.radius + cb.radius;
-        if (distance < min_dist) {
-          Body& ra = bodies[ca.parent];
-          Body& rb = bodies[cb.parent];
-          const bool distance_pushed = distance < (T)1e-6f;
-          if (distance_pushed) {
-            V2<T> push = {(T)0.01f, (T)0};
-            ra.pos = ra.pos + push;
-            rb.pos = rb.pos - push;
-            ca.snap = ra.pos + ca.off;
-            cb.snap = rb.pos + cb.off;
-            axis = ca.snap - cb.snap;
-            distance = length(axis);
-            ++pushouts;
-          }
-          V2<T> va = ra.vcalc, vb = rb.vcalc;
-          if (!ca.sensor && !cb.sensor) {
-            V2<T> n = axis / distance;
-            if (isnan2(n)) return ORACLE_NAN;  // physics.rs:293 assert
-            T delta = min_dist - distance;
-            T ratio = (T)1 - ra.mass / (ra.mass + rb.mass);
-            ra.pos = ra.pos + (ratio * delta) * n;
-            rb.pos = rb.pos - (((T)1 - ratio) * delta) * n;
-          }
-          ++count;
-          if (tracing) {
-            trace_pairs.push_back(i);
-            trace_pairs.push_back(j | (distance_pushed ? 0x80000000u : 0u));
-          }
-          if (record_events) events.push_back(Event{i, j, {(double)va.x, (double)va.y}, {(double)vb.x, (double)vb.y}});
-        }
-      }
+    if (grid_pairs) {
+      int st = grid_collisions(count);
+      if (st != ORACLE_GRID_UNUSABLE) return finish_collisions(count, st);
+      count = 0;
     }
+    for (uint32_t i = 0; i < nc; ++i)
+      for (uint32_t j = 0; j < i; ++j) {
+        int r = resolve_pair(i, j, count);
+        if (r >= 2) return r - 2;
+      }
+    return finish_collisions(count, ORACLE_OK);
+  }
+
+  int finish_collisions(uint64_t count, int st) {
     contacts += count;
     last_substep_contacts = count;
     if (tracing) trace_counts.push_back(count);
+    return st;
+  }
+
+  // The same pairs in the same order, enumerated through a uniform grid of
+  // the substep's collider snapshots instead of all C^2/2 pairs.  A contact
+  // needs |snap_i - snap_j| < r_i + r_j <= 2 r_max, and the cell edge is
+  // 2 r_max (1 + 2^-6), so every contact's partner lies in the 3x3 cells
+  // around a collider.  The colliders are counting-sorted by (row, column);
+  // a sweep in that order keeps, for each of the three neighbour rows, the
+  // range of the three neighbour cells with pointers that only move forward.
+  // The contacts found are then resolved in the reference's order: i
+  // ascending, j < i ascending.
+  // Returns ORACLE_GRID_UNUSABLE before touching any state when the grid does
+  // not fit (non-finite snapshots, more rows plus columns than 64 per
+  // collider), and ORACLE_GRID_PUSHOUT if a push-out moved two snapshots (the
+  // grid is then stale; the caller must not use this mode on such scenes).
+  int grid_collisions(uint64_t& count) {
+    const uint32_t nc = (uint32_t)cols.size();
+    if (nc < 2) return ORACLE_OK;
+    double rmax = 0, lo[2] = {HUGE_VAL, HUGE_VAL}, hi[2] = {-HUGE_VAL, -HUGE_VAL};
+    for (const Collider& c : cols) {
+      const double x = (double)c.snap.x, y = (double)c.snap.y;
+      if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite((double)c.radius)) return ORACLE_GRID_UNUSABLE;
+      rmax = std::fmax(rmax, (double)c.radius);
+      lo[0] = std::fmin(lo[0], x), lo[1] = std::fmin(lo[1], y);
+      hi[0] = std::fmax(hi[0], x), hi[1] = std::fmax(hi[1], y);
+    }
+    const double cs = rmax > 0 ? 2.0 * rmax * (1.0 + 1.0 / 64.0) : 1.0;
+    const double wd = std::floor((hi[0] - lo[0]) / cs) + 1, hd = std::floor((hi[1] - lo[1]) / cs) + 1;
+    if (!(wd + hd <= 64.0 * nc + 65536.0)) return ORACLE_GRID_UNUSABLE;
+    const uint32_t W = (uint32_t)wd, H = (uint32_t)hd;
+    // cell coordinates, then a stable counting sort by column and one by row
+    grid_gx.resize(nc), grid_gy.resize(nc), grid_tmp.resize(nc), grid_order.resize(nc);
+    for (uint32_t c = 0; c < nc; ++c) {
+      const uint32_t gx = (uint32_t)std::floor(((double)cols[c].snap.x - lo[0]) / cs);
+      const uint32_t gy = (uint32_t)std::floor(((double)cols[c].snap.y - lo[1]) / cs);
+      grid_gx[c] = gx < W ? gx : W - 1, grid_gy[c] = gy < H ? gy : H - 1;
+    }
+    auto counting_sort = [&](const std::vector<uint32_t>& key, uint32_t range, const std::vector<uint32_t>& in,
+                             std::vector<uint32_t>& out) {
+      grid_count.assign((size_t)range + 1, 0);
+      for (uint32_t c : in) ++grid_count[key[c] + 1];
+      for (uint32_t k = 0; k < range; ++k) grid_count[k + 1] += grid_count[k];
+      for (uint32_t c : in) out[grid_count[key[c]]++] = c;
+    };
+    for (uint32_t c = 0; c < nc; ++c) grid_tmp[c] = c;
+    counting_sort(grid_gx, W, grid_tmp, grid_order);
+    counting_sort(grid_gy, H, grid_order, grid_tmp);
+    // candidate records in (row, column) order, so the sweep streams them
+    grid_items.resize(nc);
+    for (uint32_t q = 0; q < nc; ++q) {
+      const uint32_t c = grid_tmp[q];
+      const Collider& k = cols[c];
+      grid_items[q] = GridItem{k.snap, k.radius, k.memb, k.filt, k.parent, c,
+                               ((uint64_t)grid_gy[c] << 32) | grid_gx[c]};
+    }
+    grid_pairs_found.clear();
+    uint32_t first[3] = {0, 0, 0}, last[3] = {0, 0, 0};  // per neighbour row: [first, last) of its 3 cells
+    for (uint32_t q = 0; q < nc; ++q) {
+      const GridItem& gi = grid_items[q];
+      const uint32_t i = gi.c;
+      const uint64_t gy = gi.key >> 32, gx = gi.key & 0xffffffffu;
+      for (int r = 0; r < 3; ++r) {
+        if (gy + r < 1) continue;  // the row below row 0
+        const uint64_t row = gy + r - 1;
+        const uint64_t k0 = (row << 32) | (gx ? gx - 1 : 0), k1 = (row << 32) | (gx + 1);
+        while (first[r] < nc && grid_items[first[r]].key < k0) ++first[r];
+        if (last[r] < first[r]) last[r] = first[r];
+        while (last[r] < nc && grid_items[last[r]].key <= k1) ++last[r];
+        for (uint32_t k = first[r]; k < last[r]; ++k) {
+          const GridItem& g = grid_items[k];
+          if (g.c >= i) continue;
+          // the same test resolve_pair makes; it is repeated there on the
+          // unchanged snapshots, so this only drops pairs that are no contact
+          if (!((gi.memb & g.filt) != 0 && (g.memb & gi.filt) != 0) || gi.parent == g.parent) continue;
+          const V2<T> axis = gi.snap - g.snap;
+          const T min_dist = gi.radius + g.radius;
+          // far pairs leave before the square root: sqrt rounds by at most
+          // half an ulp, so dot >= (1 + 2^-20) min_dist^2 means length >= min_dist
+          if ((double)dot(axis, axis) >= (double)min_dist * (double)min_dist * (1.0 + 0x1p-20)) continue;
+          if (!(length(axis) < min_dist)) continue;
+          grid_pairs_found.push_back(((uint64_t)i << 32) | g.c);
+        }
+      }
+    }
+    std::sort(grid_pairs_found.begin(), grid_pairs_found.end());
+    for (uint64_t key : grid_pairs_found) {
+      int r = resolve_pair((uint32_t)(key >> 32), (uint32_t)key, count);
+      if (r == 1) return ORACLE_GRID_PUSHOUT;
+      if (r >= 2) return r - 2;
+    }
     return ORACLE_OK;
   }
 
@@ -676,6 +798,7 @@ uint64_t oracle_world_events(void* w, uint32_t* a, uint32_t* b, double* va, doub
   return wb->events.size();
 }
 void oracle_world_clear_events(void* w) { static_cast<WorldBase*>(w)->events.clear(); }
+void oracle_world_set_grid_pairs(void* w, int on) { static_cast<WorldBase*>(w)->grid_pairs = on != 0; }
 
 // Substep trace (test infrastructure for derivative checks): on != 0 clears
 // and starts it.  Each state is 2n position, 2n position_old, 2c snapshots,

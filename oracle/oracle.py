@@ -66,6 +66,7 @@ def lib() -> ctypes.CDLL:
         "oracle_world_time": (f64, [_P]),
         "oracle_world_events": (u64, [_P, _P, _P, _P, _P, u64]),
         "oracle_world_clear_events": (None, [_P]),
+        "oracle_world_set_grid_pairs": (None, [_P, i32]),
         "oracle_world_trace": (None, [_P, i32]),
         "oracle_world_trace_states": (u64, [_P, _P, u64]),
         "oracle_world_trace_pairs": (u64, [_P, _P, u64]),
@@ -172,7 +173,13 @@ class OracleWorld:
     world: see :func:`step_batched`."""
 
     def __init__(self, scene, precision: int = 32, *, joint_order=None, record_events: bool = False,
-                 maintain_spatial_hash: bool = False, old_dt: float = 1.0):
+                 maintain_spatial_hash: bool = False, old_dt: float = 1.0, grid_pairs: bool = False):
+        """grid_pairs: enumerate the contact loop's pairs through a uniform
+        grid of the collider snapshots -- the same pairs in the same order as
+        the reference's C^2/2 loop (physics.rs:248-249), for full-size checks.
+        A push-out (coincident centres) in this mode ends the step with status
+        GRID_PUSHOUT; scenes whose extent does not fit a grid fall back to the
+        C^2/2 loop."""
         if scene.n_worlds != 1:
             raise ValueError("OracleWorld takes one world; unpack batched scenes first")
         self._keep = []
@@ -180,6 +187,8 @@ class OracleWorld:
                            maintain_spatial_hash=maintain_spatial_hash, old_dt=old_dt)
         self._h = lib().oracle_world_new(ctypes.byref(st), int(precision))
         self._keep = None
+        if grid_pairs:
+            lib().oracle_world_set_grid_pairs(self._h, 1)
         self.n_bodies = scene.n_bodies
         self.n_colliders = scene.n_colliders
         self.precision = precision

@@ -1,0 +1,101 @@
+"""Parity at the full sizes of the benchmark workloads.
+
+The oracle's grid-enumerated contact loop (the same pairs in the same order as
+the reference's C^2/2 loop, pinned to it in tests/test_oracle_grid.py) makes
+the full scenes checkable in seconds:
+
+* 1,000,000 spheres, r ~ U[0.05, 0.15], 40% packing with overlaps, dt = 1/120
+  (the benchmark world): five steps, bit-exact.
+* 4,096 uneven worlds, 64..8,192 bodies each (7.0M bodies), springs on 10%:
+  one batched step, bit-exact world by world.
+* 256 worlds x 2,048 spheres with 1,024 springs each (the differentiable
+  rollout batch): a 10-step CUDA-graph rollout, bit-exact world by world.
+* 200,000 bodies with 1-4 colliders, 50,000 fixed joints, 100,000 springs:
+  one step against the oracle run in the GPU's joint colour order; rotation
+  enters the snapshots through sin/cos and the joints through atan2 (CUDA's,
+  not glibc's), so this one is compared with a tolerance.
+"""
+import numpy as np
+import pytest
+
+from blobs_gb300 import native, scenes
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_run(scene, steps, rollout=False):
+    with native.World(scene) as w:
+        if rollout:
+            w.rollout(scene.dt, steps)
+        else:
+            for _ in range(steps):
+                w.step(scene.dt)
+        out = w.read_bodies()
+        out["snap"] = w.read_snapshots()
+        out["contacts"] = w.contact_count()[0]
+        out["joint_order"] = w.joint_order()[0] if scene.n_joints else None
+    return out
+
+
+def oracle_run(scene, steps, precision=32, joint_order=None):
+    o = oracle.OracleWorld(scene, precision, joint_order=joint_order, grid_pairs=True)
+    assert o.step(scene.dt, steps) == 0  # also: no push-out, which this mode reports
+    out = o.bodies()
+    out["snap"] = o.snapshots()
+    out["contacts"] = o.contacts
+    return out
+
+
+def assert_exact(got, want, keys=("pos", "pos_old", "vel"), what=""):
+    for k in keys:
+        bad = np.argwhere(got[k].astype(np.float64) != want[k])
+        assert len(bad) == 0, "%s %s: %d entries differ, first %s" % (what, k, len(bad), bad[:3].tolist())
+
+
+def test_million_spheres_five_steps_bit_exact():
+    s = scenes.dense_spheres(seed=2, n=1_000_000)
+    got, want = gpu_run(s, 5), oracle_run(s, 5)
+    assert want["contacts"] > 9_000_000
+    assert got["contacts"] == want["contacts"]
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+
+
+def check_batched(scene, got, steps):
+    total = 0
+    for w in range(scene.n_worlds):
+        sub = scenes.unpack_world(scene, w)
+        want = oracle_run(sub, steps)
+        b0, b1 = int(scene.world_body_offsets[w]), int(scene.world_body_offsets[w + 1])
+        assert_exact({k: got[k][b0:b1] for k in ("pos", "pos_old", "vel")}, want, what="world %d" % w)
+        total += want["contacts"]
+    assert got["contacts"] == total
+
+
+def test_uneven_batch_full_one_step_bit_exact_per_world():
+    s = scenes.uneven_batch()
+    assert s.n_worlds == 4096 and s.n_bodies > 6_000_000
+    check_batched(s, gpu_run(s, 1), 1)
+
+
+def test_gradient_batch_full_rollout_bit_exact_per_world():
+    s = scenes.gradient_batch()[0]
+    assert s.n_worlds == 256 and s.n_bodies == 256 * 2048 and s.n_springs == 256 * 1024
+    check_batched(s, gpu_run(s, 10, rollout=True), 10)
+
+
+def test_jointed_full_one_step_tolerance():
+    """Against the f32 oracle in the GPU's joint order: 99.9% of the position
+    components within 1e-4 (1 + |x|) and contact counts within 0.1%; the
+    largest deviation no larger than the f32 oracle's own from the f64 re-run
+    (a contact that flips on a one-ulp sin/cos difference moves a body by a
+    contact correction, which f32 itself does against f64)."""
+    s = scenes.jointed_bodies()
+    assert s.n_bodies == 200_000 and s.n_joints == 50_000 and s.n_springs == 100_000
+    got = gpu_run(s, 1)
+    ref32 = oracle_run(s, 1, 32, joint_order=got["joint_order"])
+    ref64 = oracle_run(s, 1, 64, joint_order=got["joint_order"])
+    err = np.abs(got["pos"].astype(np.float64) - ref32["pos"])
+    assert np.mean(err <= 1e-4 * (1.0 + np.abs(ref32["pos"]))) >= 0.999
+    assert abs(got["contacts"] - ref32["contacts"]) <= 1e-3 * ref32["contacts"]
+    assert err.max() <= 1.01 * np.abs(ref32["pos"] - ref64["pos"]).max() + 1e-3
