@@ -297,6 +297,38 @@ def general_comparison(dev, steps=10, warmup=3, seed=3):
             "body_steps_per_s": scene.n_bodies * steps / (ms / 1e3), "kernel_launches_per_step": launches}
 
 
+def literal_box_comparison(dev, steps=20, warmup=3, seed=2):
+    """The 1,000,000-sphere workload in the literal 2000 x 2000 walled box
+    (0.85% packing instead of 40%): device time of `steps` single steps after
+    `warmup`, L2 flushed before each, on the world's stream, at the
+    autotuned cell edge."""
+    import torch
+    from blobs_gb300 import native, scenes
+    scene = scenes.dense_spheres(seed=seed, n=1_000_000, literal_box=True)
+    stream = torch.cuda.current_stream(dev)
+    w = native.World(scene, device=dev.index)
+    w.set_stream(stream.cuda_stream)
+    cell_scale = w.autotune(scene, scene.dt, trial_steps=3)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        w.step(scene.dt)
+    torch.cuda.synchronize()
+    ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.step(scene.dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    contacts_total, contacts_last = w.contact_count()
+    w.close()
+    return {"bodies": scene.n_bodies, "box": float(scene.world_box[0, 2] - scene.world_box[0, 0]), "steps": steps,
+            "ms_per_step": ms / steps, "sphere_steps_per_s": scene.n_bodies * steps / (ms / 1e3),
+            "contacts_last_substep": contacts_last, "cell_scale": cell_scale}
+
+
 def adjoint_comparison(dev, steps=120, every=16, seed=5):
     """256 worlds x 2,048 spheres with 1,024 springs each,
     a 120-step forward pass (one CUDA-graph rollout) against the same
@@ -487,6 +519,8 @@ def run_ours(args):
         line["adjoint"] = adjoint_comparison(dev)
     if rank == 0 and not args.no_general:
         line["general"] = general_comparison(dev)
+    if rank == 0 and not args.no_literal:
+        line["literal_box"] = literal_box_comparison(dev)
     world.close()
     if dist is not None:
         dist.barrier()
@@ -506,6 +540,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-general", action="store_true")
+    ap.add_argument("--no-literal", action="store_true", help="skip the 2000 x 2000 literal-box run")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

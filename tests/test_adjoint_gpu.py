@@ -9,10 +9,10 @@ the f32 GPU adjoint, checked two ways:
   the comparison is tight -- every gradient within 1e-3 relative plus 1e-4
   of the largest gradient of its kind (f32 accumulation over the substeps);
 * against f64 central finite differences of the oracle (h = 1e-4 for
-  velocities, 1e-4 relative for stiffnesses) over a horizon of two steps,
-  where the f32 and f64 trajectories still resolve the same contacts:
-  within 5e-3 relative (or 5e-5 of the largest gradient of the kind) -- the
-  two trajectories already differ by f32 rounding.
+  velocities, 1e-4 relative for stiffnesses) over horizons of two and four
+  steps, where the f32 and f64 trajectories still resolve the same contacts:
+  within 1e-3 relative (or 1e-5 of the largest gradient of the kind); a
+  sample whose contact count changes within +-h is discarded.
 
 Over longer horizons the f32 and f64 trajectories drift apart by ~1e-4 and
 resolve different contacts, and the derivative of the contact correction
@@ -172,8 +172,8 @@ def world_loss_f64(sub, m, t, M, steps, dt):
     return float((d * d).sum()) / M, o.contacts
 
 
-def test_gradients_match_f64_finite_differences():
-    steps = 2
+@pytest.mark.parametrize("steps", [2, 4])
+def test_gradients_match_f64_finite_differences(steps):
     scene, marked, targets = make_scene(seed=21, n_worlds=3)
     final, g, after, gv, gk = gpu_gradients(scene, marked, targets, steps, 1)
     M = sum(len(m) for m in marked)
@@ -224,7 +224,7 @@ def test_gradients_match_f64_finite_differences():
             discarded += 1
             continue
         fd = (Lp - Lm) / (2.0 * h)
-        assert abs(g_gpu - fd) <= 5e-3 * max(abs(fd), floor), (trial, g_gpu, fd)
+        assert abs(g_gpu - fd) <= 1e-3 * max(abs(fd), floor), (trial, g_gpu, fd)
         checked += 1
     assert checked >= 16, (checked, discarded)
 
