@@ -42,6 +42,13 @@ struct WorldParam {
   uint32_t pad[2];
 };
 
+// One contact as seen from one body: its place in the reference's pair
+// sequence and the body's position increment.
+struct Contact {
+  unsigned long long key;  // (hi << 33) | (lo << 1), hi > lo collider indices
+  float2 corr;             // signed position increment for this body
+};
+
 // Every device pointer of a loaded scene.  Passed to kernels by value.
 struct WorldDev {
   uint32_t n_bodies, n_cols, n_springs, n_joints, n_worlds, n_circles, n_cells, n_tiles;
@@ -84,13 +91,23 @@ struct WorldDev {
   float* spr_k;
   float* spr_c;
 
-  // joints (stored in the coloured processing order)
+  // joints, stored in the processing order: first the joints of the small
+  // components, component by component (arena order inside each), then the
+  // joints of the large components in (colour, arena index) order
   uint32_t* jnt_a;
   uint32_t* jnt_b;
-  float2* jnt_anchor_a;
-  float2* jnt_anchor_b;
-  float* jnt_dist;
-  float* jnt_target;
+  float4* jnt_anc;           // (anchor_a, anchor_b)
+  float4* jnt_coef;          // (1/ma + 1/mb, (1/ma) / that, distance, target_angle), from the constant masses
+  uint32_t* jnt_local;       // block-local body slots a | b << 16 (small components) | JL_STATIC_A / _B
+  // small components, solved in shared memory by k_joint_blocks: block k
+  // holds components [jb_comp_start[k], jb_comp_start[k+1]) and the bodies
+  // jb_bodies[jb_body_start[k] .. jb_body_start[k+1]); component c is the
+  // joints [jb_joint_start[c], jb_joint_start[c+1]) of the processing order
+  uint32_t* jb_comp_start;
+  uint32_t* jb_joint_start;
+  uint32_t* jb_body_start;
+  uint32_t* jb_bodies;
+  uint32_t n_jblocks;
 
   float* circles;            // 3 per circle
   WorldParam* wparam;
@@ -100,6 +117,9 @@ struct WorldDev {
   uint32_t* cell_start;      // n_cells + 1
   uint32_t* rank;            // per collider: slot inside its cell
   float4* sorted;            // per slot: (x, y, radius, collider index bits)
+  Contact* clist;            // general path, per collider: up to CL_CAP contacts of the substep
+  uint8_t* ccount;           // general path, per collider: contacts in clist
+  uint8_t* bslow;            // general path, per body: contacts need the ordered walk (zero between substeps)
   uint32_t* tile_sums;       // per scan tile
 
   // single-sphere path: body storage re-sorted into cell order once per step
@@ -231,7 +251,15 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
+constexpr uint32_t CL_CAP = 8;             // general path: contacts kept per collider
 constexpr uint32_t COUNTER_BINS = 64;
 constexpr uint32_t REC_CAP = 16;           // recorded contacts per body and substep (adjoint)
+constexpr int JB_THREADS = 128;            // k_joint_blocks: one thread per small component
+constexpr uint32_t JB_MAX_JOINTS = 64;     // larger components take the coloured sweep
+constexpr uint32_t JB_JOINTS = 512;        // joints staged in shared memory per block
+constexpr uint32_t JB_BODIES = 640;        // bodies staged per block (<= JB_JOINTS + JB_THREADS)
+constexpr uint32_t JB_ITERS = 4;           // iterations whose rotation terms a block keeps
+constexpr uint32_t JL_STATIC_A = 1u << 15; // jnt_local flags: body a / b is static
+constexpr uint32_t JL_STATIC_B = 1u << 31;
 
 }  // namespace blobs

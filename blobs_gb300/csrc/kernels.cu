@@ -304,11 +304,6 @@ __device__ __forceinline__ void for_each_candidate(const WorldDev& w, const Worl
   }
 }
 
-struct Contact {
-  unsigned long long key;  // (hi << 33) | (lo << 1)
-  float2 corr;             // signed position increment for this body
-};
-
 // One contact of collider c (body b) with collider c2 (body b2), in the
 // reference's terms: a = the higher collider index (outer loop), b = lower.
 // Returns false if the pair is not in contact.  Sets *push when the
@@ -502,23 +497,129 @@ __global__ void __launch_bounds__(256) k_contact_single(WorldDev w, const float2
 }
 
 // ---------------------------------------------------------------------------
-// k_contact_general: any body / collider layout (several colliders per body,
-// offsets, groups, sensors).  One thread per body; the contacts of all its
-// colliders are merged in the reference's pair-sequence order
-// (outer collider index, then inner collider index).
+// The general contact pass: any body / collider layout (several colliders
+// per body, offsets, groups, sensors), in two kernels.
+//
+// k_collider_contacts: one thread per cell-sorted collider slot (a warp works
+// on neighbouring cells and every thread on one collider), which finds the
+// collider's contacts and keeps up to CL_CAP of them -- (pair key,
+// correction of its body) -- in clist.  A push-out, or more contacts, marks
+// the body for the ordered walk.  Counts and events are taken here.
+//
+// k_body_contacts: one thread per body, which merges its colliders' contacts
+// in the reference's pair-sequence order (outer collider index, then inner)
+// and applies them; a marked body gathers its contacts again
+// (collect_contacts), or on a push-out or a long list walks them in that
+// order (ordered_walk), which also handles the push-out branch.
 // ---------------------------------------------------------------------------
-template <bool MW, bool SPR, bool PEND, bool FUSE>
-__global__ void __launch_bounds__(256) k_contact_general(WorldDev w, const float2* __restrict__ pos_in,
-                                                         float2* __restrict__ pos_out, SubstepArgs args) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+template <bool MW>
+__global__ void __launch_bounds__(256) k_collider_contacts(WorldDev w, const float2* __restrict__ pos_in) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t ncontacts = 0, npush = 0;
-  if (b < w.n_bodies) {
-    const uint32_t c0 = w.body_col_start[b], c1 = w.body_col_start[b + 1];
-    const WorldParam wp = load_wparam(w, MW ? w.body_world[b] : 0u);
+  if (e < w.n_cols) {
+    const float4 me = w.sorted[e];
+    uint32_t c = __float_as_uint(me.w);
+    if (c >= w.n_cols) {
+      set_status(w, ST_BAD_INDEX);
+      c = 0;
+    }
+    const uint32_t b = w.col_parent[c];
+    const WorldParam wp = load_wparam(w, MW ? w.col_world[c] : 0u);
+    const float2 s = v2(me.x, me.y);  // the snapshot and radius of collider c
+    const float r = me.z;
     const float m_b = w.mass[b];
-    Contact list[CONTACT_LIST];
-    int nl = 0;
+    const uint32_t memb = w.col_memb[c], filt = w.col_filt[c];
+    const bool sens = w.col_sensor[c] != 0;
+    const float2 off = w.col_off[c];
+    Contact* out = w.clist + (size_t)c * CL_CAP;
+    uint32_t n = 0;
     bool slow = false;
+    for_each_candidate(w, wp, s, [&](uint32_t q) {
+      const float4 o = w.sorted[q];
+      const uint32_t c2 = __float_as_uint(o.w);
+      if (c2 == c || c2 >= w.n_cols) return;
+      const float2 s2 = v2(o.x, o.y);
+      // cheap distance pre-test, the exact test is repeated in contact_pair
+      const float2 ax = c > c2 ? sub(s, s2) : sub(s2, s);
+      const float md = c > c2 ? (r + o.z) : (o.z + r);
+      if (!(len2(ax) < md)) return;
+      const uint32_t b2 = w.col_parent[c2];
+      if (b2 == b) return;
+      const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
+      if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
+      const bool sens_any = sens || (w.col_sensor[c2] != 0);
+      PairOut po;
+      if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, s2, o.z, w.mass[b2], sens_any, off, w.col_off[c2], po))
+        return;
+      if (c > c2) {
+        ++ncontacts;
+        npush += po.pushed ? 1u : 0u;
+        if (w.ev_rec) record_event(w, c, c2, w.vel[b], w.vel[b2]);
+      }
+      if (po.pushed || n >= CL_CAP) {
+        slow = true;
+        return;
+      }
+      out[n].key = pair_key(c, c2);
+      out[n].corr = po.corr;
+      ++n;
+    });
+    w.ccount[c] = (uint8_t)n;
+    if (slow) w.bslow[b] = 1u;
+  }
+  count_contacts(w, ncontacts, npush);
+}
+
+// All contacts of body b's colliders into `list`, in candidate order.
+// Returns false on a push-out or more than CONTACT_LIST contacts.
+__device__ __noinline__ bool collect_contacts(const WorldDev& w, const WorldParam& wp,
+                                              const float2* __restrict__ pos_in, uint32_t b, uint32_t c0,
+                                              uint32_t c1, float m_b, Contact* list, int& nl) {
+  bool ok = true;
+  for (uint32_t qc = c0; qc < c1 && ok; ++qc) {
+    const uint32_t c = w.body_cols[qc];
+    const float2 s = w.snap[c];
+    const float r = w.col_radius[c];
+    const uint32_t memb = w.col_memb[c], filt = w.col_filt[c];
+    const bool sens = w.col_sensor[c] != 0;
+    const float2 off = w.col_off[c];
+    for_each_candidate(w, wp, s, [&](uint32_t q) {
+      if (!ok) return;
+      const float4 o = w.sorted[q];
+      const uint32_t c2 = __float_as_uint(o.w);
+      if (c2 == c || c2 >= w.n_cols) return;
+      const uint32_t b2 = w.col_parent[c2];
+      if (b2 == b) return;
+      const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
+      if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
+      const bool sens_any = sens || (w.col_sensor[c2] != 0);
+      PairOut po;
+      if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, v2(o.x, o.y), o.z, w.mass[b2], sens_any, off,
+                        w.col_off[c2], po))
+        return;
+      if (po.pushed || nl >= CONTACT_LIST) {
+        ok = false;
+        return;
+      }
+      list[nl].key = pair_key(c, c2);
+      list[nl].corr = po.corr;
+      ++nl;
+    });
+  }
+  return ok;
+}
+
+// Body b's contacts applied one by one in pair-sequence order: each round
+// selects the smallest pair key above the last one over all its colliders'
+// candidates.
+__device__ __noinline__ float2 ordered_walk(const WorldDev& w, const WorldParam& wp, const float2* __restrict__ pos_in,
+                                            uint32_t b, uint32_t c0, uint32_t c1, float m_b) {
+  float2 p = pos_in[b];
+  unsigned long long last = 0ull;
+  bool first = true;
+  while (true) {
+    unsigned long long best = ~0ull;
+    PairOut bo;
     for (uint32_t qc = c0; qc < c1; ++qc) {
       const uint32_t c = w.body_cols[qc];
       const float2 s = w.snap[c];
@@ -530,84 +631,74 @@ __global__ void __launch_bounds__(256) k_contact_general(WorldDev w, const float
         const float4 o = w.sorted[q];
         const uint32_t c2 = __float_as_uint(o.w);
         if (c2 == c || c2 >= w.n_cols) return;
-        const float2 s2 = v2(o.x, o.y);
-        // cheap distance pre-test, the exact test is repeated in contact_pair
-        const float2 ax = c > c2 ? sub(s, s2) : sub(s2, s);
-        const float md = c > c2 ? (r + o.z) : (o.z + r);
-        if (!(len2(ax) < md)) return;
+        const unsigned long long k = pair_key(c, c2);
+        if ((!first && k <= last) || k >= best) return;
         const uint32_t b2 = w.col_parent[c2];
         if (b2 == b) return;
         const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
         if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
         const bool sens_any = sens || (w.col_sensor[c2] != 0);
         PairOut po;
-        if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, s2, o.z, w.mass[b2], sens_any, off, w.col_off[c2],
-                          po))
+        if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, v2(o.x, o.y), o.z, w.mass[b2], sens_any, off,
+                          w.col_off[c2], po))
           return;
-        if (c > c2) {
-          ++ncontacts;
-          npush += po.pushed ? 1u : 0u;
-          if (w.ev_rec) record_event(w, c, c2, w.vel[b], w.vel[b2]);
-        }
-        if (po.pushed || nl >= CONTACT_LIST) {
-          slow = true;
-          return;
-        }
-        list[nl].key = pair_key(c, c2);
-        list[nl].corr = po.corr;
-        ++nl;
+        best = k;
+        bo = po;
       });
     }
-    float2 p = pos_in[b];
+    if (best == ~0ull) break;
+    if (bo.pushed) p = add(p, bo.push);
+    if (bo.has_corr) p = add(p, bo.corr);
+    last = best;
+    first = false;
+  }
+  return p;
+}
+
+template <bool MW, bool SPR, bool PEND, bool FUSE>
+__global__ void __launch_bounds__(256) k_body_contacts(WorldDev w, const float2* __restrict__ pos_in,
+                                                       float2* __restrict__ pos_out, SubstepArgs args) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.n_bodies) return;
+  const uint32_t c0 = w.body_col_start[b], c1 = w.body_col_start[b + 1];
+  float2 p = pos_in[b];
+  bool slow = w.bslow[b] != 0;
+  if (!slow) {
+    Contact list[CONTACT_LIST];
+    int nl = 0;
+    for (uint32_t qc = c0; qc < c1 && !slow; ++qc) {
+      const uint32_t c = w.body_cols[qc];
+      const uint32_t n = min((uint32_t)w.ccount[c], CL_CAP);
+      if (nl + (int)n > CONTACT_LIST) {
+        slow = true;
+        break;
+      }
+      for (uint32_t k = 0; k < n; ++k) list[nl++] = w.clist[(size_t)c * CL_CAP + k];
+    }
     if (!slow) {
       sort_contacts(list, nl);
       for (int k = 0; k < nl; ++k) p = add(p, list[k].corr);
-    } else {
-      unsigned long long last = 0ull;
-      bool first = true;
-      while (true) {
-        unsigned long long best = ~0ull;
-        PairOut bo;
-        for (uint32_t qc = c0; qc < c1; ++qc) {
-          const uint32_t c = w.body_cols[qc];
-          const float2 s = w.snap[c];
-          const float r = w.col_radius[c];
-          const uint32_t memb = w.col_memb[c], filt = w.col_filt[c];
-          const bool sens = w.col_sensor[c] != 0;
-          const float2 off = w.col_off[c];
-          for_each_candidate(w, wp, s, [&](uint32_t q) {
-            const float4 o = w.sorted[q];
-            const uint32_t c2 = __float_as_uint(o.w);
-            if (c2 == c || c2 >= w.n_cols) return;
-            const unsigned long long k = pair_key(c, c2);
-            if ((!first && k <= last) || k >= best) return;
-            const uint32_t b2 = w.col_parent[c2];
-            if (b2 == b) return;
-            const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];
-            if (!((memb & filt2) != 0u && (memb2 & filt) != 0u)) return;
-            const bool sens_any = sens || (w.col_sensor[c2] != 0);
-            PairOut po;
-            if (!contact_pair(w, pos_in, c, b, s, r, m_b, c2, b2, v2(o.x, o.y), o.z, w.mass[b2], sens_any, off,
-                              w.col_off[c2], po))
-              return;
-            best = k;
-            bo = po;
-          });
-        }
-        if (best == ~0ull) break;
-        if (bo.pushed) p = add(p, bo.push);
-        if (bo.has_corr) p = add(p, bo.corr);
-        last = best;
-        first = false;
-      }
-    }
-    if (FUSE) {
-      integrate_body<MW, SPR, PEND, false>(w, b, p, pos_out, args);
-    } else {
-      pos_out[b] = p;
     }
   }
-  count_contacts(w, ncontacts, npush);
+  if (slow) {
+    // a collider kept only part of its contacts: gather the body's contacts
+    // again, or walk them in order on a push-out or a long list
+    w.bslow[b] = 0u;
+    const WorldParam wp = load_wparam(w, MW ? w.body_world[b] : 0u);
+    Contact list[CONTACT_LIST];
+    int nl = 0;
+    if (collect_contacts(w, wp, pos_in, b, c0, c1, w.mass[b], list, nl)) {
+      sort_contacts(list, nl);
+      for (int k = 0; k < nl; ++k) p = add(p, list[k].corr);
+    } else {
+      p = ordered_walk(w, wp, pos_in, b, c0, c1, w.mass[b]);
+    }
+  }
+  if (FUSE) {
+    integrate_body<MW, SPR, PEND, false>(w, b, p, pos_out, args);
+  } else {
+    pos_out[b] = p;
+  }
 }
 
 // Advances the collision-event substep sequence (after a contact pass).
@@ -628,45 +719,171 @@ void launch_v_divide(float2* v, uint32_t n, float dt, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// k_joints: one colour of solve_fixed_joints (physics.rs:424-477).  Joints of
-// one colour touch disjoint bodies, so they run in parallel; colours run in
-// sequence, joint_iterations times.
+// One FixedJoint of solve_fixed_joints (physics.rs:430-470), in two parts:
+// joint_position moves the two bodies (physics.rs:434-461) and returns the
+// anchor difference dp; joint_rotation gives the rotation correction rc of
+// physics.rs:462-466 from dp.  Positions never depend on rotations here, so
+// the rotation part may run later, as long as each body's rotation receives
+// its rc terms in the same order.  The mass terms 1/ma + 1/mb and
+// (1/ma) / (1/ma + 1/mb) are constant and come precomputed with the same
+// IEEE operations.  joint_position returns false when the joint is skipped
+// (anchors closer than 1e-6).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ bool joint_position(float4 anc, float4 coef, uint32_t loc, float2& pa, float2& pb,
+                                               float2& dp) {
+  const float2 wa = add(pa, v2(anc.x, anc.y));
+  const float2 wb = add(pb, v2(anc.z, anc.w));
+  dp = sub(wb, wa);
+  const float distance = len2(dp);
+  if (distance < 1e-6f) return false;
+  const float off_by = distance - coef.z;
+  const float2 correction = divs(v2(off_by * dp.x, off_by * dp.y), distance);
+  const float ims = coef.x;
+  if (loc & JL_STATIC_A) {
+    pb = sub(pb, mul(correction, ims));
+  } else if (loc & JL_STATIC_B) {
+    pa = add(pa, mul(correction, ims));
+  } else {
+    const float ratio = coef.y;
+    pa = add(pa, mul(correction, ratio));
+    pb = sub(pb, mul(correction, 1.0f - ratio));
+  }
+  return true;
+}
+
+__device__ __forceinline__ float joint_rotation(float2 dp, float target) {
+  const float angle_a = atan2f(dp.y, dp.x);
+  const float angle_b = -atan2f(dp.y, -dp.x);  // physics.rs:464 precedence
+  return ((angle_b - angle_a) - target) * 0.5f;
+}
+
+__device__ __forceinline__ bool fixed_joint(float4 anc, float4 coef, uint32_t loc, float2& pa, float2& pb, float& ra,
+                                            float& rb, float dt) {
+  float2 dp;
+  if (!joint_position(anc, coef, loc, pa, pb, dp)) return false;
+  const float rc = joint_rotation(dp, coef.w);
+  ra = ra + rc * dt;
+  rb = rb - rc * dt;
+  return true;
+}
+
+// k_joints: one colour of the large components' joints.  Joints of one
+// colour touch disjoint bodies, so they run in parallel; colours run in
+// sequence, joint_iterations times.
 __global__ void __launch_bounds__(256) k_joints(WorldDev w, float2* __restrict__ pos, uint32_t j0, uint32_t j1,
                                                 float dt) {
   const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= j1) return;
   const uint32_t ia = w.jnt_a[j], ib = w.jnt_b[j];
   float2 pa = pos[ia], pb = pos[ib];
-  const float2 wa = add(pa, w.jnt_anchor_a[j]);
-  const float2 wb = add(pb, w.jnt_anchor_b[j]);
-  const float2 dp = sub(wb, wa);
-  const float distance = len2(dp);
-  if (distance < 1e-6f) return;
-  const float off_by = distance - w.jnt_dist[j];
-  const float2 correction = divs(v2(off_by * dp.x, off_by * dp.y), distance);
-  const float ma = w.mass[ia], mb = w.mass[ib];
-  const float ims = (1.0f / ma) + (1.0f / mb);
-  const bool sa = (w.bflags[ia] & BF_STATIC) != 0, sb = (w.bflags[ib] & BF_STATIC) != 0;
-  if (sa) {
-    pb = sub(pb, mul(correction, ims));
-  } else if (sb) {
-    pa = add(pa, mul(correction, ims));
-  } else {
-    const float ratio = (1.0f / ma) / ims;
-    pa = add(pa, mul(correction, ratio));
-    pb = sub(pb, mul(correction, 1.0f - ratio));
-  }
+  float ra = w.rot[ia], rb = w.rot[ib];
+  if (!fixed_joint(w.jnt_anc[j], w.jnt_coef[j], w.jnt_local[j], pa, pb, ra, rb, dt)) return;
   pos[ia] = pa;
   pos[ib] = pb;
-  const float angle_a = atan2f(dp.y, dp.x);
-  const float angle_b = -atan2f(dp.y, -dp.x);  // physics.rs:464 precedence
-  const float rc = ((angle_b - angle_a) - w.jnt_target[j]) * 0.5f;
-  const float ra = w.rot[ia] + rc * dt;
-  const float rb = w.rot[ib] - rc * dt;
   w.rot[ia] = ra;
   w.rot[ib] = rb;
   if (!isfinite(ra) || !isfinite(rb)) set_status(w, ST_NAN);
+}
+
+// k_joint_blocks: the small components.  A component's joints touch no body
+// of another component, so each component runs alone -- all iterations, its
+// joints in the reference's arena order -- which gives every body exactly
+// the sequence of updates of the reference's sweep.  One thread per
+// component; the block's bodies and joints are staged in shared memory.  Up
+// to JB_ITERS iterations the sweep runs in three passes, so that the
+// sequential chain of a component carries only the position arithmetic:
+// (1) per component, the position sweep, keeping every (iteration, joint)
+// dp; (2) the rotation corrections of all of them in parallel; (3) per
+// component, the rotations summed in the sweep's order.
+__global__ void __launch_bounds__(JB_THREADS) k_joint_blocks(WorldDev w, float2* __restrict__ pos, float dt,
+                                                             uint32_t iterations) {
+  __shared__ float2 s_pos[JB_BODIES];
+  __shared__ float s_rot[JB_BODIES];
+  __shared__ float4 s_anc[JB_JOINTS];
+  __shared__ float4 s_coef[JB_JOINTS];
+  __shared__ uint32_t s_loc[JB_JOINTS];
+  __shared__ float2 s_dp[JB_ITERS * JB_JOINTS];  // dp of (iteration, joint); then rc in .x
+  __shared__ uint8_t s_on[JB_ITERS * JB_JOINTS];  // the joint was applied (not skipped)
+  const uint32_t k = blockIdx.x;
+  const uint32_t b0 = w.jb_body_start[k], nbody = min(w.jb_body_start[k + 1] - b0, JB_BODIES);
+  const uint32_t c0 = w.jb_comp_start[k], c1 = w.jb_comp_start[k + 1];
+  const uint32_t qa = w.jb_joint_start[c0], njoint = min(w.jb_joint_start[c1] - qa, JB_JOINTS);
+  for (uint32_t i = threadIdx.x; i < nbody; i += JB_THREADS) {
+    const uint32_t body = w.jb_bodies[b0 + i];
+    s_pos[i] = pos[body];
+    s_rot[i] = w.rot[body];
+  }
+  for (uint32_t i = threadIdx.x; i < njoint; i += JB_THREADS) {
+    s_anc[i] = w.jnt_anc[qa + i];
+    s_coef[i] = w.jnt_coef[qa + i];
+    s_loc[i] = w.jnt_local[qa + i];
+  }
+  __syncthreads();
+  const uint32_t c = c0 + threadIdx.x;
+  const bool mine = c < c1;
+  const uint32_t q0 = mine ? w.jb_joint_start[c] - qa : 0u, q1 = mine ? w.jb_joint_start[c + 1] - qa : 0u;
+  bool bad = q1 > njoint, nan = false;
+  for (uint32_t q = q0; q < q1 && !bad; ++q) {
+    const uint32_t loc = s_loc[q];
+    bad = (loc & 0x7fffu) >= nbody || ((loc >> 16) & 0x7fffu) >= nbody;
+  }
+  const bool split = iterations <= JB_ITERS;
+  if (mine && !bad) {
+    for (uint32_t it = 0; it < iterations; ++it)
+      for (uint32_t q = q0; q < q1; ++q) {
+        const uint32_t loc = s_loc[q];
+        const uint32_t la = loc & 0x7fffu, lb = (loc >> 16) & 0x7fffu;
+        float2 pa = s_pos[la], pb = s_pos[lb];
+        if (split) {
+          float2 dp;
+          const bool on = joint_position(s_anc[q], s_coef[q], loc, pa, pb, dp);
+          s_dp[it * JB_JOINTS + q] = dp;
+          s_on[it * JB_JOINTS + q] = on ? 1 : 0;
+          if (!on) continue;
+          s_pos[la] = pa;
+          s_pos[lb] = pb;
+        } else {
+          float ra = s_rot[la], rb = s_rot[lb];
+          if (!fixed_joint(s_anc[q], s_coef[q], loc, pa, pb, ra, rb, dt)) continue;
+          s_pos[la] = pa;
+          s_pos[lb] = pb;
+          s_rot[la] = ra;
+          s_rot[lb] = rb;
+          nan = nan || !isfinite(ra) || !isfinite(rb);
+        }
+      }
+  }
+  if (split) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < iterations * njoint; i += JB_THREADS) {
+      const uint32_t it = i / njoint, q = i - it * njoint, e = it * JB_JOINTS + q;
+      if (s_on[e]) s_dp[e].x = joint_rotation(s_dp[e], s_coef[q].w);
+    }
+    __syncthreads();
+    if (mine && !bad) {
+      for (uint32_t it = 0; it < iterations; ++it)
+        for (uint32_t q = q0; q < q1; ++q) {
+          const uint32_t e = it * JB_JOINTS + q;
+          if (!s_on[e]) continue;
+          const uint32_t loc = s_loc[q];
+          const uint32_t la = loc & 0x7fffu, lb = (loc >> 16) & 0x7fffu;
+          const float rc = s_dp[e].x;
+          const float ra = s_rot[la] + rc * dt;
+          const float rb = s_rot[lb] - rc * dt;
+          s_rot[la] = ra;
+          s_rot[lb] = rb;
+          nan = nan || !isfinite(ra) || !isfinite(rb);
+        }
+    }
+  }
+  if (mine && bad) set_status(w, ST_BAD_INDEX);
+  if (nan) set_status(w, ST_NAN);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < nbody; i += JB_THREADS) {
+    const uint32_t body = w.jb_bodies[b0 + i];
+    pos[body] = s_pos[i];
+    w.rot[body] = s_rot[i];
+  }
 }
 
 template <bool MW, bool SPR, bool PEND, bool SINGLE>
@@ -766,25 +983,36 @@ void launch_scatter_forces(const WorldDev& w, const float2* pos, bool mw, bool s
         BLOBS_DISPATCH_BOOL(pending, PE, k_scatter_forces<MW, SC, SP, PE><<<g, 256, 0, st>>>(w, pos)))));
 }
 
-void launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
+uint32_t launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, bool mw, bool single, bool springs,
                      bool pending, bool fuse, float dt, float old_dt, bool do_keys, bool rot_dynamic,
                      cudaStream_t st) {
   SubstepArgs a{dt, old_dt, dt / old_dt, dt / dt, do_keys ? 1u : 0u, rot_dynamic ? 1u : 0u};
   if (single) {
-    if (!w.n_cols) return;
+    if (!w.n_cols) return 0u;
     const uint32_t g = blocks_for(w.n_cols, 256);
     BLOBS_DISPATCH_BOOL(mw, MW,
       BLOBS_DISPATCH_BOOL(springs, SP,
         BLOBS_DISPATCH_BOOL(pending, PE,
           BLOBS_DISPATCH_BOOL(fuse, FU, k_contact_single<MW, SP, PE, FU><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
   } else {
-    if (!w.n_bodies) return;
+    if (!w.n_bodies) return 0u;
+    if (w.n_cols) {
+      const uint32_t gc = blocks_for(w.n_cols, 256);
+      BLOBS_DISPATCH_BOOL(mw, MW, k_collider_contacts<MW><<<gc, 256, 0, st>>>(w, pos_in));
+    }
     const uint32_t g = blocks_for(w.n_bodies, 256);
     BLOBS_DISPATCH_BOOL(mw, MW,
       BLOBS_DISPATCH_BOOL(springs, SP,
         BLOBS_DISPATCH_BOOL(pending, PE,
-          BLOBS_DISPATCH_BOOL(fuse, FU, k_contact_general<MW, SP, PE, FU><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+          BLOBS_DISPATCH_BOOL(fuse, FU, k_body_contacts<MW, SP, PE, FU><<<g, 256, 0, st>>>(w, pos_in, pos_out, a)))));
+    return w.n_cols ? 2u : 1u;
   }
+  return 1u;
+}
+
+void launch_joint_blocks(const WorldDev& w, float2* pos, float dt, uint32_t iterations, cudaStream_t st) {
+  if (!w.n_jblocks) return;
+  k_joint_blocks<<<w.n_jblocks, JB_THREADS, 0, st>>>(w, pos, dt, iterations);
 }
 
 void launch_joints(const WorldDev& w, float2* pos, uint32_t j0, uint32_t j1, float dt, cudaStream_t st) {

@@ -224,14 +224,16 @@ namespace {
 // scene validation + derived host arrays
 // ---------------------------------------------------------------------------
 struct HostScene {
-  std::vector<float2> pos, pos_old, pend_acc, vel, vreq, col_off, snap, anchor_a, anchor_b;
+  std::vector<float2> pos, pos_old, pend_acc, vel, vreq, col_off, snap;
+  std::vector<float4> jnt_anc, jnt_coef;
   std::vector<float> rot, angvel, pend_torque, mass, inertia, gmod, bound_r, col_radius, spr_rest, spr_k, spr_c,
-      jnt_dist, jnt_target, circles;
+      circles;
   std::vector<uint8_t> bflags, col_sensor;
   std::vector<uint32_t> body_world, col_world, body_col_start, body_cols, body_spr_start, body_spr, col_parent,
       col_memb, col_filt, spr_a, spr_b, jnt_a, jnt_b;
   std::vector<WorldParam> wparam;
   std::vector<uint32_t> colour_offsets, joint_order;
+  std::vector<uint32_t> jb_comp_start, jb_joint_start, jb_body_start, jb_bodies, jnt_local;
   uint32_t n_cells = 0;
   bool single = false, rot_dynamic = false, pending = false, any_dynamic = false;
 };
@@ -403,49 +405,139 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
     }
   }
 
-  // joints: greedy colouring in arena order, processing order = (colour, arena index)
-  std::vector<uint32_t> colour(nj, 0);
+  // joints: the bodies a chain of joints links form a component, and the
+  // joints of one component touch no body of another, so each component can
+  // be swept on its own -- every iteration, its joints in arena order --
+  // giving each body the reference's sequence of updates (physics.rs:428-431).
+  // Components of at most JB_MAX_JOINTS joints become one thread each of
+  // k_joint_blocks (shared memory, reference order); the joints of larger
+  // ones are greedily coloured in arena order and swept colour by colour.
+  // Processing order: small components (largest first, so a warp's threads
+  // carry similar loads), then the large components' joints by (colour,
+  // arena index).
+  std::vector<uint32_t> uf(nb);
+  for (uint32_t i = 0; i < nb; ++i) uf[i] = i;
+  auto find = [&](uint32_t x) {
+    while (uf[x] != x) x = uf[x] = uf[uf[x]];
+    return x;
+  };
+  for (uint32_t j = 0; j < nj; ++j) {
+    const uint32_t a = s.jnt_a[j], b = s.jnt_b[j];
+    if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
+    if (h.body_world[a] != h.body_world[b]) return BLOBS_ERR_INVALID_ARGUMENT;
+    if (nw > 1 && (uint32_t)world_of(s.world_joint_offsets, nw, j) != h.body_world[a])
+      return BLOBS_ERR_INVALID_ARGUMENT;
+    const uint32_t ra = find(a), rb = find(b);
+    if (ra != rb) uf[std::max(ra, rb)] = std::min(ra, rb);
+  }
+  std::vector<uint32_t> comp_joints(nj ? nb : 0, 0), comp_first(nj ? nb : 0, 0xffffffffu);
+  for (uint32_t j = 0; j < nj; ++j) {
+    const uint32_t r = find(s.jnt_a[j]);
+    if (comp_joints[r]++ == 0) comp_first[r] = j;
+  }
+  std::vector<uint32_t> small;  // roots of the small components, in processing order
+  for (uint32_t r = 0; r < (nj ? nb : 0); ++r)
+    if (comp_joints[r] && comp_joints[r] <= JB_MAX_JOINTS) small.push_back(r);
+  std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
+    return comp_joints[x] != comp_joints[y] ? comp_joints[x] > comp_joints[y] : comp_first[x] < comp_first[y];
+  });
+  std::vector<uint32_t> comp_index(nj ? nb : 0, 0xffffffffu);
+  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) comp_index[small[c]] = c;
+  h.jb_joint_start.assign(small.size() + 1, 0);
+  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c)
+    h.jb_joint_start[c + 1] = h.jb_joint_start[c] + comp_joints[small[c]];
+  const uint32_t n_small = small.empty() ? 0u : h.jb_joint_start.back();
+  h.joint_order.assign(nj, 0);
+  std::vector<uint32_t> large;  // the large components' joints, arena order
+  {
+    std::vector<uint32_t> fill(h.jb_joint_start.begin(), h.jb_joint_start.end() - (small.empty() ? 0 : 1));
+    for (uint32_t j = 0; j < nj; ++j) {
+      const uint32_t c = comp_index[find(s.jnt_a[j])];
+      if (c != 0xffffffffu) h.joint_order[fill[c]++] = j;
+      else large.push_back(j);
+    }
+  }
+  // blocks of at most JB_THREADS components and JB_BODIES bodies, with each
+  // body's block-local slot
+  h.jb_comp_start.assign(1, 0);
+  h.jb_body_start.assign(1, 0);
+  h.jb_bodies.clear();
+  h.jnt_local.assign(nj, 0);
+  {
+    std::vector<int32_t> slot(nj ? nb : 0, -1);
+    uint32_t comps_in_block = 0;
+    auto close_block = [&]() {
+      for (uint32_t i = h.jb_body_start.back(); i < (uint32_t)h.jb_bodies.size(); ++i) slot[h.jb_bodies[i]] = -1;
+      h.jb_comp_start.push_back(h.jb_comp_start.back() + comps_in_block);
+      h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
+      comps_in_block = 0;
+    };
+    for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) {
+      const uint32_t q0 = h.jb_joint_start[c], q1 = h.jb_joint_start[c + 1];
+      // a component of n joints has at most n + 1 distinct bodies (it is connected)
+      const uint32_t in_block = (uint32_t)h.jb_bodies.size() - h.jb_body_start.back();
+      const uint32_t joints_in_block = q0 - h.jb_joint_start[h.jb_comp_start.back()];
+      if (comps_in_block == (uint32_t)JB_THREADS || in_block + (q1 - q0) + 1 > JB_BODIES ||
+          joints_in_block + (q1 - q0) > JB_JOINTS)
+        close_block();
+      for (uint32_t q = q0; q < q1; ++q) {
+        const uint32_t j = h.joint_order[q];
+        uint32_t loc[2];
+        const uint32_t ends[2] = {s.jnt_a[j], s.jnt_b[j]};
+        for (int e2 = 0; e2 < 2; ++e2) {
+          if (slot[ends[e2]] < 0) {
+            slot[ends[e2]] = (int32_t)((uint32_t)h.jb_bodies.size() - h.jb_body_start.back());
+            h.jb_bodies.push_back(ends[e2]);
+          }
+          loc[e2] = (uint32_t)slot[ends[e2]];
+        }
+        h.jnt_local[q] = loc[0] | (loc[1] << 16);
+      }
+      ++comps_in_block;
+    }
+    if (comps_in_block) close_block();
+  }
+  // the large components: greedy colouring in arena order
+  std::vector<uint32_t> colour(large.size(), 0);
   uint32_t n_colours = 0;
   {
-    std::vector<std::vector<uint32_t>> used(nb);
-    for (uint32_t j = 0; j < nj; ++j) {
-      const uint32_t a = s.jnt_a[j], b = s.jnt_b[j];
-      if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
-      if (h.body_world[a] != h.body_world[b]) return BLOBS_ERR_INVALID_ARGUMENT;
-      if (nw > 1 && (uint32_t)world_of(s.world_joint_offsets, nw, j) != h.body_world[a])
-        return BLOBS_ERR_INVALID_ARGUMENT;
+    std::vector<std::vector<uint32_t>> used(large.empty() ? 0 : nb);
+    for (size_t i = 0; i < large.size(); ++i) {
+      const uint32_t a = s.jnt_a[large[i]], b = s.jnt_b[large[i]];
       uint32_t k = 0;
       while (std::find(used[a].begin(), used[a].end(), k) != used[a].end() ||
              std::find(used[b].begin(), used[b].end(), k) != used[b].end())
         ++k;
-      colour[j] = k;
+      colour[i] = k;
       used[a].push_back(k);
       used[b].push_back(k);
       n_colours = std::max(n_colours, k + 1);
     }
   }
-  h.colour_offsets.assign(n_colours + 1, 0);
-  for (uint32_t j = 0; j < nj; ++j) h.colour_offsets[colour[j] + 1]++;
-  for (uint32_t k = 0; k < n_colours; ++k) h.colour_offsets[k + 1] += h.colour_offsets[k];
-  h.joint_order.resize(nj);
+  h.colour_offsets.assign(n_colours + 1, n_small);
+  for (size_t i = 0; i < large.size(); ++i) h.colour_offsets[colour[i] + 1]++;
+  for (uint32_t k = 0; k < n_colours; ++k) h.colour_offsets[k + 1] += h.colour_offsets[k] - n_small;
   {
     std::vector<uint32_t> fill(h.colour_offsets.begin(), h.colour_offsets.end() - 1);
-    for (uint32_t j = 0; j < nj; ++j) h.joint_order[fill[colour[j]]++] = j;
+    for (size_t i = 0; i < large.size(); ++i) h.joint_order[fill[colour[i]]++] = large[i];
   }
   h.jnt_a.resize(nj);
   h.jnt_b.resize(nj);
-  h.anchor_a.resize(nj);
-  h.anchor_b.resize(nj);
-  h.jnt_dist.resize(nj);
-  h.jnt_target.resize(nj);
+  h.jnt_anc.resize(nj);
+  h.jnt_coef.resize(nj);
   for (uint32_t q = 0; q < nj; ++q) {
     const uint32_t j = h.joint_order[q];
-    h.jnt_a[q] = s.jnt_a[j];
-    h.jnt_b[q] = s.jnt_b[j];
-    h.anchor_a[q] = v2(s.jnt_anchor_a[2 * j], s.jnt_anchor_a[2 * j + 1]);
-    h.anchor_b[q] = v2(s.jnt_anchor_b[2 * j], s.jnt_anchor_b[2 * j + 1]);
-    h.jnt_dist[q] = s.jnt_distance[j];
-    h.jnt_target[q] = s.jnt_target[j];
+    const uint32_t a = s.jnt_a[j], b = s.jnt_b[j];
+    h.jnt_a[q] = a;
+    h.jnt_b[q] = b;
+    h.jnt_anc[q] = make_float4(s.jnt_anchor_a[2 * j], s.jnt_anchor_a[2 * j + 1], s.jnt_anchor_b[2 * j],
+                               s.jnt_anchor_b[2 * j + 1]);
+    // physics.rs:445-452 mass terms, IEEE f32 as the device would compute them
+    const float inv_a = 1.0f / h.mass[a];
+    const float ims = inv_a + (1.0f / h.mass[b]);
+    h.jnt_coef[q] = make_float4(ims, inv_a / ims, s.jnt_distance[j], s.jnt_target[j]);
+    if (h.bflags[a] & BF_STATIC) h.jnt_local[q] |= JL_STATIC_A;
+    if (h.bflags[b] & BF_STATIC) h.jnt_local[q] |= JL_STATIC_B;
   }
   if (nj) h.rot_dynamic = true;
 
@@ -512,6 +604,7 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
     if (cell_base >= (1ull << 31)) return BLOBS_ERR_INVALID_ARGUMENT;
   }
   h.n_cells = (uint32_t)cell_base;
+
   return BLOBS_OK;
 }
 
@@ -521,8 +614,9 @@ template <class T> cudaError_t up(T* dst, const std::vector<T>& src, cudaStream_
 }
 
 // Lay out (or size) every device array of the scene.
-void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t nb, uint32_t nc, uint32_t ns,
-           uint32_t nj, uint32_t nw, uint32_t ncirc, uint32_t n_cells, uint32_t n_tiles, bool sorted_storage) {
+void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, const HostScene& h, uint32_t nb, uint32_t nc,
+           uint32_t ns, uint32_t nj, uint32_t nw, uint32_t ncirc, uint32_t n_cells, uint32_t n_tiles,
+           bool sorted_storage) {
   const uint32_t ss = sorted_storage ? nb : 0u;
   d.sa[0] = cv.take<float4>(ss);
   d.sa[1] = cv.take<float4>(ss);
@@ -570,16 +664,22 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, uint32_t 
   d.spr_c = cv.take<float>(ns);
   d.jnt_a = cv.take<uint32_t>(nj);
   d.jnt_b = cv.take<uint32_t>(nj);
-  d.jnt_anchor_a = cv.take<float2>(nj);
-  d.jnt_anchor_b = cv.take<float2>(nj);
-  d.jnt_dist = cv.take<float>(nj);
-  d.jnt_target = cv.take<float>(nj);
+  d.jnt_anc = cv.take<float4>(nj);
+  d.jnt_coef = cv.take<float4>(nj);
+  d.jb_comp_start = cv.take<uint32_t>(h.jb_comp_start.size());
+  d.jb_joint_start = cv.take<uint32_t>(h.jb_joint_start.size());
+  d.jb_body_start = cv.take<uint32_t>(h.jb_body_start.size());
+  d.jb_bodies = cv.take<uint32_t>(h.jb_bodies.size());
+  d.jnt_local = cv.take<uint32_t>(h.jnt_local.size());
   d.circles = cv.take<float>(3 * (size_t)ncirc);
   d.wparam = cv.take<WorldParam>(nw);
   d.cell_count = cv.take<uint32_t>(n_cells);
   d.cell_start = cv.take<uint32_t>((size_t)n_cells + 1);
   d.rank = cv.take<uint32_t>(nc);
   d.sorted = cv.take<float4>(sorted_storage ? 0u : nc);
+  d.clist = cv.take<Contact>(sorted_storage ? 0u : (size_t)nc * CL_CAP);
+  d.ccount = cv.take<uint8_t>(sorted_storage ? 0u : nc);
+  d.bslow = cv.take<uint8_t>(sorted_storage ? 0u : nb);
   d.tile_sums = cv.take<uint32_t>(n_tiles);
   *counters = cv.take<Counters>(1);
 }
@@ -619,6 +719,10 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
   const uint64_t n_colours = w->colour_offsets.empty() ? 0 : w->colour_offsets.size() - 1;
   auto joints = [&](float2* p) {
     mark_begin(w, PHASE_JOINTS);
+    if (d.n_jblocks && w->cfg.joint_iterations) {
+      launch_joint_blocks(d, p, dt, w->cfg.joint_iterations, st);
+      w->enqueued += 1;
+    }
     for (uint32_t it = 0; it < w->cfg.joint_iterations; ++it)
       for (size_t k = 0; k < n_colours; ++k) launch_joints(d, p, w->colour_offsets[k], w->colour_offsets[k + 1], dt, st);
     w->enqueued += (uint64_t)w->cfg.joint_iterations * n_colours;
@@ -716,10 +820,9 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     // integration would overwrite in place
     const bool fuse = !w->has_joints && !w->events_on;
     mark_begin(w, PHASE_CONTACT);
-    launch_contacts(d, in, out, w->multiworld, w->single, w->has_springs, pending, fuse, dt, old_dt, true,
-                    w->rot_dynamic, st);
+    w->enqueued += launch_contacts(d, in, out, w->multiworld, w->single, w->has_springs, pending, fuse, dt, old_dt,
+                                   true, w->rot_dynamic, st);
     mark_end(w);
-    w->enqueued += 1;
     if (d.ev_rec) {
       launch_ev_tick(d, st);
       w->enqueued += 1;
@@ -1002,12 +1105,12 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
     h.wparam[0].first_dyn = first_dyn;
     h.wparam[0].uniform_gmod = nb ? h.gmod[0] : 1.0f;
   }
-  carve(sizer, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
+  carve(sizer, d, w->pos, &counters, h, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   e = cudaMalloc(&w->arena, sizer.off + 256);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   Carver cv;
   cv.base = static_cast<char*>(w->arena);
-  carve(cv, d, w->pos, &counters, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
+  carve(cv, d, w->pos, &counters, h, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   d.n_bodies = nb;
   d.n_cols = nc;
   d.n_springs = ns;
@@ -1016,6 +1119,7 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   d.n_circles = ncirc;
   d.n_cells = h.n_cells;
   d.n_tiles = n_tiles;
+  d.n_jblocks = h.jb_comp_start.empty() ? 0u : (uint32_t)h.jb_comp_start.size() - 1u;
   d.gravity = v2(w->cfg.gravity[0], w->cfg.gravity[1]);
   d.contacts_total = counters->contacts_total;
   d.pushouts_total = counters->pushouts_total;
@@ -1060,10 +1164,13 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   UP(d.spr_c, h.spr_c);
   UP(d.jnt_a, h.jnt_a);
   UP(d.jnt_b, h.jnt_b);
-  UP(d.jnt_anchor_a, h.anchor_a);
-  UP(d.jnt_anchor_b, h.anchor_b);
-  UP(d.jnt_dist, h.jnt_dist);
-  UP(d.jnt_target, h.jnt_target);
+  UP(d.jnt_anc, h.jnt_anc);
+  UP(d.jnt_coef, h.jnt_coef);
+  UP(d.jb_comp_start, h.jb_comp_start);
+  UP(d.jb_joint_start, h.jb_joint_start);
+  UP(d.jb_body_start, h.jb_body_start);
+  UP(d.jb_bodies, h.jb_bodies);
+  UP(d.jnt_local, h.jnt_local);
   UP(d.circles, h.circles);
   UP(d.wparam, h.wparam);
 #undef UP
@@ -1095,6 +1202,7 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
     if (e == cudaSuccess) e = up(d.where, ident, s);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)h.n_cells, s);
+  if (e == cudaSuccess && !sorted_storage) e = cudaMemsetAsync(d.bslow, 0, nb, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(Counters), s);
   if (e != cudaSuccess) {
     cudaFree(w->arena);

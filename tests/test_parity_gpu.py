@@ -162,6 +162,25 @@ def test_multi_collider_bodies_bit_exact():
     assert got["contacts"] == want["contacts"]
 
 
+def test_pushout_on_the_general_path():
+    """Multi-collider bodies with two colliders at the same point: the push-out
+    branch (physics.rs:272-286) on the general contact path, bit-exact (no
+    earlier contact of either body in the substep)."""
+    s = scenes.spheres([[0.0, 0.0], [0.0, 0.0], [5.0, 5.0], [-5.0, 3.0]], [0.1, 0.1, 0.2, 0.15], gravity=(0.0, 0.0))
+    # a second collider on bodies 1 and 3, away from the coincident pair
+    s.col_parent = np.concatenate([s.col_parent, np.array([1, 3], np.uint32)])
+    s.col_offset = np.concatenate([s.col_offset, np.array([[0.6, 0.0], [0.0, 0.4]], np.float32)])
+    s.col_radius = np.concatenate([s.col_radius, np.array([0.1, 0.12], np.float32)])
+    s.col_mass_override = np.concatenate([s.col_mass_override, np.full(2, np.nan, np.float32)])
+    s.col_sensor = np.concatenate([s.col_sensor, np.zeros(2, np.uint8)])
+    s.col_memb = np.concatenate([s.col_memb, np.full(2, scenes.ALL_GROUPS, np.uint32)])
+    s.col_filt = np.concatenate([s.col_filt, np.full(2, scenes.ALL_GROUPS, np.uint32)])
+    assert not s.single_collider()
+    got, want = run_gpu(s, 1), run_oracle(s, 1)
+    assert want["pushouts"] == 1 and got["pushouts"] == 1
+    assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+
+
 def test_circle_constraint_bit_exact():
     s = scenes.sparse_spheres(seed=12, n=400)
     s.world_box = None
@@ -193,6 +212,50 @@ def test_joints_single_collider_positions_exact_in_gpu_order():
     want = run_oracle(s, 3, joint_order=got["joint_order"])
     assert_exact(got, want)
     np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
+
+
+def test_joints_small_components_exact_in_reference_order():
+    """Joint components of at most 64 joints are swept one by one, each in
+    the reference's arena order, which gives every body the reference's own
+    sequence of updates: positions are bit-exact against the oracle run in
+    the reference's joint order (joints created in a shuffled order, so the
+    arena order is not sorted by body)."""
+    rng = np.random.Generator(np.random.PCG64(6))
+    s = scenes.random_world(rng, 4000, 0.1, 0.25, 0.2, 0.5)
+    near = scenes._pairs_within(s.pos, 1.0)
+    pick = rng.choice(len(near), 1500, replace=False)  # unsorted: shuffled arena order
+    scenes.add_fixed_joints(s, near[pick, 0], near[pick, 1])
+    got = run_gpu(s, 3)
+    want = run_oracle(s, 3)
+    assert_exact(got, want)
+    np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
+
+
+def test_joints_long_chain_beside_small_components():
+    """A 300-body chain (one component of 299 joints: the coloured sweep)
+    beside small components (swept one by one): positions bit-exact against
+    the oracle run in the GPU's processing order."""
+    rng = np.random.Generator(np.random.PCG64(16))
+    s = scenes.random_world(rng, 3000, 0.1, 0.25, 0.2, 0.5)
+    chain = rng.permutation(3000)[:300]
+    rest = np.setdiff1d(np.arange(3000), chain)
+    near = scenes._pairs_within(s.pos, 1.0)
+    near = near[np.isin(near[:, 0], rest) & np.isin(near[:, 1], rest)]
+    pick = rng.choice(len(near), 800, replace=False)
+    a = np.concatenate([chain[:-1], near[pick, 0]])
+    b = np.concatenate([chain[1:], near[pick, 1]])
+    order = rng.permutation(len(a))
+    scenes.add_fixed_joints(s, a[order], b[order])
+    got = run_gpu(s, 3)
+    assert native_colours(s) > 1
+    want = run_oracle(s, 3, joint_order=got["joint_order"])
+    assert_exact(got, want)
+    np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
+
+
+def native_colours(scene):
+    with native.World(scene) as w:
+        return int(w.joint_order()[1])
 
 
 def test_jointed_scaled_tolerance():
