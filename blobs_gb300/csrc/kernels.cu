@@ -808,15 +808,25 @@ __global__ void __launch_bounds__(JB_THREADS) k_joint_blocks(WorldDev w, float2*
   const uint32_t b0 = w.jb_body_start[k], nbody = min(w.jb_body_start[k + 1] - b0, JB_BODIES);
   const uint32_t c0 = w.jb_comp_start[k], c1 = w.jb_comp_start[k + 1];
   const uint32_t qa = w.jb_joint_start[c0], njoint = min(w.jb_joint_start[c1] - qa, JB_JOINTS);
-  for (uint32_t i = threadIdx.x; i < nbody; i += JB_THREADS) {
-    const uint32_t body = w.jb_bodies[b0 + i];
-    s_pos[i] = pos[body];
-    s_rot[i] = w.rot[body];
+  // staging loops unrolled to their bounds, so that all their loads are in
+  // flight together
+#pragma unroll
+  for (uint32_t r = 0; r < (JB_BODIES + JB_THREADS - 1) / JB_THREADS; ++r) {
+    const uint32_t i = threadIdx.x + r * JB_THREADS;
+    if (i < nbody) {
+      const uint32_t body = w.jb_bodies[b0 + i];
+      s_pos[i] = pos[body];
+      s_rot[i] = w.rot[body];
+    }
   }
-  for (uint32_t i = threadIdx.x; i < njoint; i += JB_THREADS) {
-    s_anc[i] = w.jnt_anc[qa + i];
-    s_coef[i] = w.jnt_coef[qa + i];
-    s_loc[i] = w.jnt_local[qa + i];
+#pragma unroll
+  for (uint32_t r = 0; r < (JB_JOINTS + JB_THREADS - 1) / JB_THREADS; ++r) {
+    const uint32_t i = threadIdx.x + r * JB_THREADS;
+    if (i < njoint) {
+      s_anc[i] = w.jnt_anc[qa + i];
+      s_coef[i] = w.jnt_coef[qa + i];
+      s_loc[i] = w.jnt_local[qa + i];
+    }
   }
   __syncthreads();
   const uint32_t c = c0 + threadIdx.x;
@@ -879,10 +889,14 @@ __global__ void __launch_bounds__(JB_THREADS) k_joint_blocks(WorldDev w, float2*
   if (mine && bad) set_status(w, ST_BAD_INDEX);
   if (nan) set_status(w, ST_NAN);
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < nbody; i += JB_THREADS) {
-    const uint32_t body = w.jb_bodies[b0 + i];
-    pos[body] = s_pos[i];
-    w.rot[body] = s_rot[i];
+#pragma unroll
+  for (uint32_t r = 0; r < (JB_BODIES + JB_THREADS - 1) / JB_THREADS; ++r) {
+    const uint32_t i = threadIdx.x + r * JB_THREADS;
+    if (i < nbody) {
+      const uint32_t body = w.jb_bodies[b0 + i];
+      pos[body] = s_pos[i];
+      w.rot[body] = s_rot[i];
+    }
   }
 }
 

@@ -412,9 +412,8 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
   // Components of at most JB_MAX_JOINTS joints become one thread each of
   // k_joint_blocks (shared memory, reference order); the joints of larger
   // ones are greedily coloured in arena order and swept colour by colour.
-  // Processing order: small components (largest first, so a warp's threads
-  // carry similar loads), then the large components' joints by (colour,
-  // arena index).
+  // Processing order: small components block by block, then the large
+  // components' joints by (colour, arena index).
   std::vector<uint32_t> uf(nb);
   for (uint32_t i = 0; i < nb; ++i) uf[i] = i;
   auto find = [&](uint32_t x) {
@@ -441,6 +440,49 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
   std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
     return comp_joints[x] != comp_joints[y] ? comp_joints[x] > comp_joints[y] : comp_first[x] < comp_first[y];
   });
+  // Deal the components, largest first, over the blocks in snake order, so
+  // that the largest (the longest sequential sweeps) land in different blocks
+  // and every block gets a similar share of the work; inside a block they stay
+  // largest first.  A component of n joints has at most n + 1 bodies.
+  std::vector<uint32_t> block_first(1, 0);  // component index at which each block starts (in `small`)
+  if (!small.empty()) {
+    uint64_t tot_j = 0;
+    for (uint32_t r : small) tot_j += comp_joints[r];
+    uint64_t nblk = std::max<uint64_t>({(small.size() + JB_THREADS - 1) / JB_THREADS,
+                                        (tot_j * 4 + 3 * JB_JOINTS - 1) / (3 * JB_JOINTS),
+                                        ((tot_j + small.size()) * 4 + 3 * JB_BODIES - 1) / (3 * JB_BODIES), 1});
+    std::vector<std::vector<uint32_t>> dealt;
+    while (true) {
+      nblk = std::min<uint64_t>(nblk, small.size());
+      dealt.assign(nblk, {});
+      std::vector<uint32_t> nj_in(nblk, 0), nb_in(nblk, 0);
+      bool fits = true;
+      for (size_t i = 0; i < small.size() && fits; ++i) {
+        const uint64_t round = i / nblk, pos = i % nblk;
+        uint64_t k = (round & 1) ? nblk - 1 - pos : pos;
+        const uint32_t cj = comp_joints[small[i]];
+        uint64_t tries = 0;
+        while (dealt[k].size() == (size_t)JB_THREADS || nj_in[k] + cj > JB_JOINTS || nb_in[k] + cj + 1 > JB_BODIES) {
+          k = (k + 1) % nblk;
+          if (++tries == nblk) {
+            fits = false;
+            break;
+          }
+        }
+        if (!fits) break;
+        dealt[k].push_back(small[i]);
+        nj_in[k] += cj;
+        nb_in[k] += cj + 1;
+      }
+      if (fits) break;
+      nblk += nblk / 8 + 1;
+    }
+    small.clear();
+    for (const auto& d : dealt) {
+      small.insert(small.end(), d.begin(), d.end());
+      block_first.push_back((uint32_t)small.size());
+    }
+  }
   std::vector<uint32_t> comp_index(nj ? nb : 0, 0xffffffffu);
   for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) comp_index[small[c]] = c;
   h.jb_joint_start.assign(small.size() + 1, 0);
@@ -457,29 +499,21 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
       else large.push_back(j);
     }
   }
-  // blocks of at most JB_THREADS components and JB_BODIES bodies, with each
-  // body's block-local slot
-  h.jb_comp_start.assign(1, 0);
+  // the blocks' bodies, each with its block-local slot
+  h.jb_comp_start.assign(block_first.begin(), block_first.end());
   h.jb_body_start.assign(1, 0);
   h.jb_bodies.clear();
   h.jnt_local.assign(nj, 0);
   {
     std::vector<int32_t> slot(nj ? nb : 0, -1);
-    uint32_t comps_in_block = 0;
-    auto close_block = [&]() {
-      for (uint32_t i = h.jb_body_start.back(); i < (uint32_t)h.jb_bodies.size(); ++i) slot[h.jb_bodies[i]] = -1;
-      h.jb_comp_start.push_back(h.jb_comp_start.back() + comps_in_block);
-      h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
-      comps_in_block = 0;
-    };
+    size_t blk = 0;
     for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) {
+      if (c == block_first[blk + 1]) {
+        for (uint32_t i = h.jb_body_start.back(); i < (uint32_t)h.jb_bodies.size(); ++i) slot[h.jb_bodies[i]] = -1;
+        h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
+        ++blk;
+      }
       const uint32_t q0 = h.jb_joint_start[c], q1 = h.jb_joint_start[c + 1];
-      // a component of n joints has at most n + 1 distinct bodies (it is connected)
-      const uint32_t in_block = (uint32_t)h.jb_bodies.size() - h.jb_body_start.back();
-      const uint32_t joints_in_block = q0 - h.jb_joint_start[h.jb_comp_start.back()];
-      if (comps_in_block == (uint32_t)JB_THREADS || in_block + (q1 - q0) + 1 > JB_BODIES ||
-          joints_in_block + (q1 - q0) > JB_JOINTS)
-        close_block();
       for (uint32_t q = q0; q < q1; ++q) {
         const uint32_t j = h.joint_order[q];
         uint32_t loc[2];
@@ -493,9 +527,8 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
         }
         h.jnt_local[q] = loc[0] | (loc[1] << 16);
       }
-      ++comps_in_block;
     }
-    if (comps_in_block) close_block();
+    if (!small.empty()) h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
   }
   // the large components: greedy colouring in arena order
   std::vector<uint32_t> colour(large.size(), 0);
