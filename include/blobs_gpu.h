@@ -226,8 +226,13 @@ int blobs_world_grid(blobs_world* w, uint32_t world, float* cell_size, float* in
                      uint32_t* log2_width, uint32_t* log2_height);
 /* Physics.time and the accumulator of fixed_step. */
 int blobs_world_time(blobs_world* w, double* time, double* accumulator);
-/* The joint processing order the GPU schedule uses (graph colouring: joints
- * sorted by colour, then by arena index).  `order` holds n_joints entries. */
+/* The joint processing order of the GPU schedule: the joints of components
+ * of at most 64 joints, component by component, each in arena order (which
+ * gives every body the reference's own sequence of updates), then the joints
+ * of larger components by graph colour, then arena index.  Sweeping the
+ * joints in this order, joint_iterations times, reproduces the GPU's result.
+ * `order` holds n_joints entries; `n_colours` counts the large components'
+ * colours (0 when every component is small). */
 int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours);
 
 /* ---- differentiable rollout (no counterpart in the reference) ---------------- */
