@@ -498,11 +498,21 @@ template <class T> class World : public WorldBase {
       if (st != ORACLE_GRID_UNUSABLE) return finish_collisions(count, st);
       count = 0;
     }
-    for (uint32_t i = 0; i < nc; ++i)
+    for (uint32_t i = 0; i < nc; ++i) {
+      // the rejection tests of resolve_pair inline, so the C^2/2 loop pays
+      // for the call only on contacts (it repeats them on the same values)
+      const uint32_t memb = cols[i].memb, filt = cols[i].filt, parent = cols[i].parent;
+      const T radius = cols[i].radius;
+      V2<T> snap = cols[i].snap;
       for (uint32_t j = 0; j < i; ++j) {
+        const Collider& cb = cols[j];
+        if (!((memb & cb.filt) != 0 && (cb.memb & filt) != 0) || parent == cb.parent) continue;
+        if (!(length(snap - cb.snap) < radius + cb.radius)) continue;
         int r = resolve_pair(i, j, count);
         if (r >= 2) return r - 2;
+        snap = cols[i].snap;  // a push-out refreshes collider i's snapshot
       }
+    }
     return finish_collisions(count, ORACLE_OK);
   }
 
