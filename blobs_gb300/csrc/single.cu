@@ -222,7 +222,8 @@ __device__ __forceinline__ BodyConst body_const(const WorldDev& w, const WorldPa
 
 // Exact selection walk over all candidates of the segments, in ascending
 // arena id (many candidates, or any layout): O(contacts x candidates).
-template <int MODE>
+// HOOKS: the adjoint's contact recording or the event stream may be on.
+template <int MODE, bool HOOKS>
 __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Segments& g, uint32_t j, uint32_t c,
                                 float2 p0, float2 s, float r, float m, uint32_t& ncontacts, uint32_t& npush,
                                 uint32_t& nrec) {
@@ -253,11 +254,11 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
     single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp);
     if (sp.pushed) p = add(p, sp.push);
     p = add(p, sp.corr);
-    if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
+    if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
     if (best < c) {
       ++ncontacts;
       npush += sp.pushed ? 1u : 0u;
-      if (w.ev_rec) single_event(w, a, c, j, best);
+      if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
     }
     last = best;
     first = false;
@@ -299,7 +300,9 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
   cand[j] = a_in[i];
 }
 
-template <int MODE>
+// HOOKS: compiled with the adjoint's contact recording and the collision
+// event stream (the plain step leaves their branches out).
+template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t ncontacts = 0, npush = 0;
@@ -372,15 +375,15 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
           p = add(p, sp.corr);
-          if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
+          if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
-            if (w.ev_rec) single_event(w, a, c, j, best);
+            if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
-        p = contacts_walk<MODE>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+        p = contacts_walk<MODE, HOOKS>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
       }
     } else if (a.contacts) {
       // cells on the grid edge (the torus wraps): general segments
@@ -423,19 +426,19 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
           p = add(p, sp.corr);
-          if (a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
+          if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
           if (best < c) {
             ++ncontacts;
             npush += sp.pushed ? 1u : 0u;
-            if (w.ev_rec) single_event(w, a, c, j, best);
+            if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
           }
         }
       } else {
-        p = contacts_walk<MODE>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+        p = contacts_walk<MODE, HOOKS>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
       }
     }
 
-    if (a.rec_list) {
+    if (HOOKS && a.rec_list) {
       a.rec_n[c] = nrec;
       if (nrec) atomicMax(a.rec_max, nrec);
     }
@@ -601,9 +604,15 @@ void launch_scatter_cand(const WorldDev& w, const float4* a_in, float4* cand, cu
 void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st) {
   if (!w.n_bodies) return;
   const uint32_t g = nblocks(w.n_bodies);
-  if (mode == 0) k_step_single<0><<<g, 256, 0, st>>>(w, a);
-  else if (mode == 1) k_step_single<1><<<g, 256, 0, st>>>(w, a);
-  else k_step_single<2><<<g, 256, 0, st>>>(w, a);
+  if (a.rec_list || w.ev_rec) {
+    if (mode == 0) k_step_single<0, true><<<g, 256, 0, st>>>(w, a);
+    else if (mode == 1) k_step_single<1, true><<<g, 256, 0, st>>>(w, a);
+    else k_step_single<2, true><<<g, 256, 0, st>>>(w, a);
+  } else {
+    if (mode == 0) k_step_single<0, false><<<g, 256, 0, st>>>(w, a);
+    else if (mode == 1) k_step_single<1, false><<<g, 256, 0, st>>>(w, a);
+    else k_step_single<2, false><<<g, 256, 0, st>>>(w, a);
+  }
 }
 
 void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st) {
