@@ -160,6 +160,15 @@ __device__ __host__ __forceinline__ float2 divs(float2 a, float s) { return v2(a
 __device__ __host__ __forceinline__ float dot2(float2 a, float2 b) { return (a.x * b.x) + (a.y * b.y); }
 __device__ __host__ __forceinline__ float len2(float2 a) { return sqrtf(dot2(a, a)); }
 
+// Pre-test of the reference's contact test (physics.rs:264-269),
+// sqrt(d.d) < ra + rb, without the square root: T >= (ra + rb)^2 strictly,
+// so d.d > T implies sqrt(d.d) >= ra + rb and the reference rejects too.
+__device__ __host__ __forceinline__ bool near_pair(float dx, float dy, float mind) {
+  const float D = (dx * dx) + (dy * dy);
+  const float T = (mind * mind) * 1.00000024f;
+  return !(D > T);
+}
+
 // Rust `(v / cs).floor() as i32`: IEEE division, saturating conversion, NaN -> 0
 // (spatial.rs:57-62 semantics).
 __device__ __host__ __forceinline__ int32_t cell_coord(float v, float cs) {

@@ -438,6 +438,7 @@ __global__ void __launch_bounds__(256) k_contact_single(WorldDev w, const float2
       const float4 o = w.sorted[q];
       const uint32_t c2 = __float_as_uint(o.w);
       if (c2 >= w.n_cols) return;
+      if (!near_pair(s.x - o.x, s.y - o.y, r + o.z)) return;  // the exact test is made in contact_pair
       PairOut po;
       if (!contact_pair(w, pos_in, c, c, s, r, m_c, c2, c2, v2(o.x, o.y), o.z, w.mass[c2], false,
                         v2(0.0f, 0.0f), v2(0.0f, 0.0f), po))
@@ -539,10 +540,8 @@ __global__ void __launch_bounds__(256) k_collider_contacts(WorldDev w, const flo
       const uint32_t c2 = __float_as_uint(o.w);
       if (c2 == c || c2 >= w.n_cols) return;
       const float2 s2 = v2(o.x, o.y);
-      // cheap distance pre-test, the exact test is repeated in contact_pair
-      const float2 ax = c > c2 ? sub(s, s2) : sub(s2, s);
-      const float md = c > c2 ? (r + o.z) : (o.z + r);
-      if (!(len2(ax) < md)) return;
+      // squared-distance pre-test; the exact test is made in contact_pair
+      if (!near_pair(s.x - s2.x, s.y - s2.y, r + o.z)) return;
       const uint32_t b2 = w.col_parent[c2];
       if (b2 == b) return;
       const uint32_t memb2 = w.col_memb[c2], filt2 = w.col_filt[c2];

@@ -80,7 +80,6 @@ __device__ __forceinline__ uint32_t slot_of(const Segments& g, uint32_t t) {
 
 // Near test of four consecutive candidate positions [q, q + 4) clipped to
 // `en`, loads issued together for memory-level parallelism.
-__device__ __forceinline__ bool near_pair(float dx, float dy, float mind);
 
 __device__ __forceinline__ void near_range(const float4* __restrict__ C, float2 s, float r, uint32_t self,
                                            uint32_t st, uint32_t en, uint32_t& t, unsigned long long& near) {
@@ -97,15 +96,6 @@ __device__ __forceinline__ void near_range(const float4* __restrict__ C, float2 
     if (near_pair(s.x - o3.x, s.y - o3.y, r + o3.z) && __float_as_uint(o3.w) != self) m |= 8u;
     if (m) near |= (unsigned long long)m << t;
   }
-}
-
-// Exact contact test of the reference (physics.rs:264-269): sqrt(d.d) < ra + rb.
-// A squared-distance test rejects first: T >= (ra + rb)^2 strictly, so
-// d.d > T implies sqrt(d.d) >= ra + rb and the reference rejects too.
-__device__ __forceinline__ bool near_pair(float dx, float dy, float mind) {
-  const float D = (dx * dx) + (dy * dy);
-  const float T = (mind * mind) * 1.00000024f;
-  return !(D > T);
 }
 
 struct SinglePair {
