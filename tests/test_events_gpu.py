@@ -138,7 +138,7 @@ def test_drain_without_events_is_a_state_error():
 
 def test_events_with_fixed_joints_in_gpu_order():
     """Single-collider bodies with fixed joints take the joint path's contact
-    kernel; against the oracle run in the GPU's joint colour order the events
+    kernel; against the oracle run in the GPU's joint processing order the events
     (pairs, order, impact velocities) are bit-exact."""
     rng = np.random.Generator(np.random.PCG64(48))
     s = scenes.random_world(rng, 1500, 0.1, 0.25, 0.25, 0.5)

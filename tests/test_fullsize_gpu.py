@@ -11,7 +11,7 @@ the full scenes checkable in seconds:
 * 256 worlds x 2,048 spheres with 1,024 springs each (the differentiable
   rollout batch): a 10-step CUDA-graph rollout, bit-exact world by world.
 * 200,000 bodies with 1-4 colliders, 50,000 fixed joints, 100,000 springs:
-  one step against the oracle run in the GPU's joint colour order; rotation
+  one step against the oracle run in the GPU's joint processing order; rotation
   enters the snapshots through sin/cos and the joints through atan2 (CUDA's,
   not glibc's), so this one is compared with a tolerance.
 """

@@ -197,11 +197,11 @@ def test_collisions_disabled_bit_exact():
     assert got["contacts"] == 0
 
 
-# ---- joints: coloured Gauss-Seidel --------------------------------------------
+# ---- joints: per component, or coloured for large components ------------------
 
 def test_joints_single_collider_positions_exact_in_gpu_order():
     """Single-collider bodies: snapshots do not depend on rotation, so the
-    positions are bit-exact against the oracle run in the GPU's colour order;
+    positions are bit-exact against the oracle run in the GPU's processing order;
     rotations use CUDA atan2f (tolerance 1e-5 rad)."""
     rng = np.random.Generator(np.random.PCG64(6))
     s = scenes.random_world(rng, 4000, 0.1, 0.25, 0.2, 0.5)
