@@ -4,6 +4,7 @@ world (Physics::step = 8 substeps at dt = 1/120, r ~ U[0.05, 0.15], 40%
 packing with overlaps, walled box, seeded synthetic scene).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --section general|batched [--steps K] [--warmup W]
 
 One JSON line on rank 0.  `value` is device-timed (CUDA events on the
 world's stream, L2 flushed between steps, inputs resident in HBM) over steps
@@ -15,7 +16,9 @@ algorithmic bytes per launch over its event-timed duration; `cpu_baseline`
 is the oracle (the CPU restatement of the reference step) on bounded samples
 of the same workload, extrapolated with the reference's O(N^2) cost model.
 With --gpus N > 1 (torchrun) every rank steps its own independent world
-(replicas; the path has no data exchange).
+(replicas; the path has no data exchange).  --section runs one secondary
+workload alone (the 200k-body jointed world, or the 4,096 batched worlds)
+with per-phase timing: the driver of the launch lists under profiles/.
 """
 from __future__ import annotations
 
@@ -165,6 +168,51 @@ def job_throughput(bodies_per_rank, steps, world_size, total_ms):
     """Whole-job sphere-steps/s: every rank steps its own world of
     `bodies_per_rank` bodies `steps` times; the job takes `total_ms`."""
     return world_size * bodies_per_rank * steps / (total_ms / 1e3)
+
+
+def run_section(args):
+    """--section general|batched: one workload alone on one GPU (the launch
+    lists and kernel captures under profiles/ are taken of this): `warmup`
+    steps, `steps` steps with per-phase CUDA events captured into the step
+    graph, then `steps` steps timed with CUDA events, L2 flushed before each;
+    one JSON line."""
+    import torch
+    from blobs_gb300 import native, scenes
+    scene = {"general": lambda: scenes.jointed_bodies(),
+             "batched": lambda: scenes.uneven_batch()}[args.section]()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    w = native.World(scene, device=0)
+    w.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        w.step(scene.dt)
+    w.set_timing(True)
+    w.step(scene.dt)  # captures the instrumented graph
+    w.phase_times()
+    phase = {}
+    for _ in range(args.steps):
+        flush.zero_()
+        w.step(scene.dt)
+        for k, (ms, _n) in w.phase_times().items():
+            phase[k] = phase.get(k, 0.0) + ms
+    w.set_timing(False)
+    ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.step(scene.dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    w.close()
+    print(json.dumps({"section": args.section, "bodies": scene.n_bodies, "colliders": scene.n_colliders,
+                      "worlds": scene.n_worlds, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": ms / args.steps,
+                      "phase_us_per_substep": {k: 1e3 * v / args.steps / scene.substeps for k, v in phase.items()}}),
+          flush=True)
 
 
 def run_reference(args):
@@ -541,10 +589,14 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-general", action="store_true")
     ap.add_argument("--no-literal", action="store_true", help="skip the 2000 x 2000 literal-box run")
+    ap.add_argument("--section", choices=["general", "batched"], default=None,
+                    help="run one secondary workload alone (profiling driver), print its phase times")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.section:
+        run_section(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
