@@ -214,14 +214,17 @@ def test_joints_single_collider_positions_exact_in_gpu_order():
     np.testing.assert_allclose(got["rotation"], want["rotation"], atol=1e-5)
 
 
-def test_joints_small_components_exact_in_reference_order():
+@pytest.mark.parametrize("iterations", [4, 0, 1, 7])
+def test_joints_small_components_exact_in_reference_order(iterations):
     """Joint components of at most 64 joints are swept one by one, each in
     the reference's arena order, which gives every body the reference's own
     sequence of updates: positions are bit-exact against the oracle run in
     the reference's joint order (joints created in a shuffled order, so the
-    arena order is not sorted by body)."""
+    arena order is not sorted by body).  Up to 4 iterations the sweep defers
+    the rotations to a second pass; 7 takes the single-pass sweep."""
     rng = np.random.Generator(np.random.PCG64(6))
     s = scenes.random_world(rng, 4000, 0.1, 0.25, 0.2, 0.5)
+    s.joint_iterations = iterations
     near = scenes._pairs_within(s.pos, 1.0)
     pick = rng.choice(len(near), 1500, replace=False)  # unsorted: shuffled arena order
     scenes.add_fixed_joints(s, near[pick, 0], near[pick, 1])
