@@ -235,6 +235,7 @@ struct SingleArgs {
   float dt, ratio_first, ratio_rest;
   uint32_t contacts, pending, springs, rot_dynamic, do_keys, write_v, move_v;
   uint32_t v_vel;            // V holds calculated_velocity (else the displacement of the last substep)
+  uint32_t mass4r;           // every body's mass is 4 x its radius: a partner's mass follows from its candidate record
   // contact recording for the adjoint (NULL in ordinary steps): every
   // contact of body c in the order it was applied (ascending partner id),
   // rec_list[k * n_bodies + c] = partner | pushed << 31 for k < REC_CAP,

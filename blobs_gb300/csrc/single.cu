@@ -239,7 +239,7 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
       }
     }
     if (!found) break;
-    const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
+    const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
     SinglePair sp;
     single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp);
     if (sp.pushed) p = add(p, sp.push);
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           }
           near &= ~best_bit;
           if (best >= w.n_bodies || best == c) continue;
-          const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
+          const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
           SinglePair sp;
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
           }
           near &= ~best_bit;
           if (best >= w.n_bodies || best == c) continue;
-          const float m2 = MODE == 0 ? bo.z * 4.0f : w.body_c[best].x;
+          const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
           SinglePair sp;
           if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
           if (sp.pushed) p = add(p, sp.push);

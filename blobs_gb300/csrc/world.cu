@@ -121,6 +121,7 @@ struct blobs_world {
   int vbuf = 0;                 // sorted storage, V untracked: the V buffer in use
   bool pending = false;
   bool keys_valid = false;
+  bool mass4r = false;          // sorted storage, every body's mass = 4 x radius
   std::vector<uint32_t> colour_offsets;  // colour k = joints [colour_offsets[k], colour_offsets[k+1]) in processing order
   std::vector<uint32_t> joint_order;     // processing position -> arena index
   float old_dt = 1.0f;
@@ -776,6 +777,7 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.write_v = last_in_step ? 1u : 0u;
     a.move_v = w->v_tracks() ? 1u : 0u;
     a.v_vel = w->v_tracks() ? 1u : 0u;
+    a.mass4r = w->mass4r ? 1u : 0u;
     a.rec_list = w->rec_list;
     a.rec_n = w->rec_n;
     a.rec_max = w->rec_max;
@@ -1126,6 +1128,9 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   Carver sizer;
   const bool sorted_storage = h.single && nj == 0;
   // a uniform single-sphere world needs no per-body constant record
+  bool mass4r = sorted_storage;  // rigid_body.rs:96-128 with one collider, no override: m = 4 r
+  for (uint32_t i = 0; i < nb && mass4r; ++i) mass4r = h.mass[i] == h.col_radius[i] * 4.0f;
+  w->mass4r = mass4r;
   bool uniform = sorted_storage && nw == 1;
   uint32_t first_dyn = 0xffffffffu;
   for (uint32_t i = 0; i < nb && uniform; ++i) {
