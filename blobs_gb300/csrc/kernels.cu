@@ -1,15 +1,23 @@
-// kernels.cu -- sm_103a kernels of one blobs substep (physics.rs:397-422).
+// kernels.cu -- sm_103a kernels of one blobs substep (physics.rs:397-422)
+// on the general path (several colliders per body, offsets, groups, sensors,
+// joints), and the cell scan both paths share.  The single-sphere path's
+// kernels are in single.cu.
 //
 // Per substep, for every packed world at once:
-//   k_cell_scan        exclusive scan of the per-cell collider counts -> cell
-//                      ranges (decoupled look-back, single pass), counts reset
+//   k_tile_sums,       exclusive scan of the per-cell collider counts -> cell
+//   k_scan_apply       ranges (two wait-free kernels), counts reset
 //   k_scatter_forces   counting-sort scatter of the colliders into cell order
 //                      (the one-digit LSD radix pass over the cell key) and,
 //                      when springs exist, gravity + spring forces per body
-//   k_contact_*        per-body gather of sphere contacts over the 3x3 cells,
-//                      corrections applied in the reference's pair-sequence
-//                      order; fused with integration when there are no joints
-//   k_joints           one colour of the fixed-joint Gauss-Seidel sweep
+//   k_collider_contacts  per cell-sorted collider: its contacts over the 3x3
+//                      cells (pair key, correction of its body)
+//   k_body_contacts    per body: its colliders' contacts applied in the
+//                      reference's pair-sequence order; fused with
+//                      integration when there are no joints
+//   k_contact_single   both passes in one for single-collider bodies
+//   k_joint_blocks     the small joint components, each swept alone in the
+//                      reference's order in shared memory
+//   k_joints           one colour of the large components' joints
 //   k_integrate        Verlet + collider snapshot + constraints, and the cell
 //                      key / rank of every collider for the next substep
 //

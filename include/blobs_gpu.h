@@ -46,7 +46,7 @@ typedef enum blobs_status {
   BLOBS_ERR_OVERFLOW = 3,         /* a caller-provided capacity was too small */
   BLOBS_ERR_NAN = 4,              /* NaN contact normal / non-finite rotation (physics.rs:293,471-474) */
   BLOBS_ERR_CUDA = 5,             /* a CUDA runtime call failed */
-  BLOBS_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+  BLOBS_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up (reserved: no kernel waits on another) */
   BLOBS_ERR_NO_DEVICE = 7,        /* no usable CUDA device */
   BLOBS_ERR_OUT_OF_MEMORY = 8,    /* device allocation failed */
   BLOBS_ERR_STATE = 9             /* call not valid in the world's current state */
