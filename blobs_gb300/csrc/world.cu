@@ -258,6 +258,170 @@ bool check_offsets(const uint32_t* off, uint32_t nw, uint32_t total) {
   return true;
 }
 
+// How a scene's joints are swept (physics.rs:424-477).  joint_order maps
+// processing position -> arena index; the first jb_joint_start.back() of them
+// belong to the small components, block k holding components
+// [jb_comp_start[k], jb_comp_start[k+1]) and bodies
+// jb_bodies[jb_body_start[k] .. jb_body_start[k+1]); jnt_local[q] holds the
+// block-local slots a | b << 16 of a small component's joint; colour k of the
+// large components is [colour_offsets[k], colour_offsets[k+1]).
+struct JointSchedule {
+  std::vector<uint32_t> joint_order, colour_offsets, jb_comp_start, jb_joint_start, jb_body_start, jb_bodies,
+      jnt_local;
+};
+
+// The joint processing schedule (see JointSchedule).  The bodies a chain
+// of joints links form a component, and the
+// joints of one component touch no body of another, so each component can
+// be swept on its own -- every iteration, its joints in arena order --
+// giving each body the reference's sequence of updates (physics.rs:428-431).
+// Components of at most JB_MAX_JOINTS joints become one thread each of
+// k_joint_blocks (shared memory, reference order); the joints of larger
+// ones are greedily coloured in arena order and swept colour by colour.
+// Processing order: small components block by block, then the large
+// components' joints by (colour, arena index).
+int joint_schedule(uint32_t nb, uint32_t nj, const uint32_t* ja, const uint32_t* jb, JointSchedule& out) {
+  std::vector<uint32_t> uf(nb);
+  for (uint32_t i = 0; i < nb; ++i) uf[i] = i;
+  auto find = [&](uint32_t x) {
+    while (uf[x] != x) x = uf[x] = uf[uf[x]];
+    return x;
+  };
+  for (uint32_t j = 0; j < nj; ++j) {
+    const uint32_t a = ja[j], b = jb[j];
+    if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
+    const uint32_t ra = find(a), rb = find(b);
+    if (ra != rb) uf[std::max(ra, rb)] = std::min(ra, rb);
+  }
+  std::vector<uint32_t> comp_joints(nj ? nb : 0, 0), comp_first(nj ? nb : 0, 0xffffffffu);
+  for (uint32_t j = 0; j < nj; ++j) {
+    const uint32_t r = find(ja[j]);
+    if (comp_joints[r]++ == 0) comp_first[r] = j;
+  }
+  std::vector<uint32_t> small;  // roots of the small components, in processing order
+  for (uint32_t r = 0; r < (nj ? nb : 0); ++r)
+    if (comp_joints[r] && comp_joints[r] <= JB_MAX_JOINTS) small.push_back(r);
+  std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
+    return comp_joints[x] != comp_joints[y] ? comp_joints[x] > comp_joints[y] : comp_first[x] < comp_first[y];
+  });
+  // Deal the components, largest first, over the blocks in snake order, so
+  // that the largest (the longest sequential sweeps) land in different blocks
+  // and every block gets a similar share of the work; inside a block they stay
+  // largest first.  A component of n joints has at most n + 1 bodies.
+  std::vector<uint32_t> block_first(1, 0);  // component index at which each block starts (in `small`)
+  if (!small.empty()) {
+    uint64_t tot_j = 0;
+    for (uint32_t r : small) tot_j += comp_joints[r];
+    uint64_t nblk = std::max<uint64_t>({(small.size() + JB_THREADS - 1) / JB_THREADS,
+                                        (tot_j * 4 + 3 * JB_JOINTS - 1) / (3 * JB_JOINTS),
+                                        ((tot_j + small.size()) * 4 + 3 * JB_BODIES - 1) / (3 * JB_BODIES), 1});
+    std::vector<std::vector<uint32_t>> dealt;
+    while (true) {
+      nblk = std::min<uint64_t>(nblk, small.size());
+      dealt.assign(nblk, {});
+      std::vector<uint32_t> nj_in(nblk, 0), nb_in(nblk, 0);
+      bool fits = true;
+      for (size_t i = 0; i < small.size() && fits; ++i) {
+        const uint64_t round = i / nblk, pos = i % nblk;
+        uint64_t k = (round & 1) ? nblk - 1 - pos : pos;
+        const uint32_t cj = comp_joints[small[i]];
+        uint64_t tries = 0;
+        while (dealt[k].size() == (size_t)JB_THREADS || nj_in[k] + cj > JB_JOINTS || nb_in[k] + cj + 1 > JB_BODIES) {
+          k = (k + 1) % nblk;
+          if (++tries == nblk) {
+            fits = false;
+            break;
+          }
+        }
+        if (!fits) break;
+        dealt[k].push_back(small[i]);
+        nj_in[k] += cj;
+        nb_in[k] += cj + 1;
+      }
+      if (fits) break;
+      nblk += nblk / 8 + 1;
+    }
+    small.clear();
+    for (const auto& d : dealt) {
+      small.insert(small.end(), d.begin(), d.end());
+      block_first.push_back((uint32_t)small.size());
+    }
+  }
+  std::vector<uint32_t> comp_index(nj ? nb : 0, 0xffffffffu);
+  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) comp_index[small[c]] = c;
+  out.jb_joint_start.assign(small.size() + 1, 0);
+  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c)
+    out.jb_joint_start[c + 1] = out.jb_joint_start[c] + comp_joints[small[c]];
+  const uint32_t n_small = small.empty() ? 0u : out.jb_joint_start.back();
+  out.joint_order.assign(nj, 0);
+  std::vector<uint32_t> large;  // the large components' joints, arena order
+  {
+    std::vector<uint32_t> fill(out.jb_joint_start.begin(), out.jb_joint_start.end() - (small.empty() ? 0 : 1));
+    for (uint32_t j = 0; j < nj; ++j) {
+      const uint32_t c = comp_index[find(ja[j])];
+      if (c != 0xffffffffu) out.joint_order[fill[c]++] = j;
+      else large.push_back(j);
+    }
+  }
+  // the blocks' bodies, each with its block-local slot
+  out.jb_comp_start.assign(block_first.begin(), block_first.end());
+  out.jb_body_start.assign(1, 0);
+  out.jb_bodies.clear();
+  out.jnt_local.assign(nj, 0);
+  {
+    std::vector<int32_t> slot(nj ? nb : 0, -1);
+    size_t blk = 0;
+    for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) {
+      if (c == block_first[blk + 1]) {
+        for (uint32_t i = out.jb_body_start.back(); i < (uint32_t)out.jb_bodies.size(); ++i)
+          slot[out.jb_bodies[i]] = -1;
+        out.jb_body_start.push_back((uint32_t)out.jb_bodies.size());
+        ++blk;
+      }
+      const uint32_t q0 = out.jb_joint_start[c], q1 = out.jb_joint_start[c + 1];
+      for (uint32_t q = q0; q < q1; ++q) {
+        const uint32_t j = out.joint_order[q];
+        uint32_t loc[2];
+        const uint32_t ends[2] = {ja[j], jb[j]};
+        for (int e2 = 0; e2 < 2; ++e2) {
+          if (slot[ends[e2]] < 0) {
+            slot[ends[e2]] = (int32_t)((uint32_t)out.jb_bodies.size() - out.jb_body_start.back());
+            out.jb_bodies.push_back(ends[e2]);
+          }
+          loc[e2] = (uint32_t)slot[ends[e2]];
+        }
+        out.jnt_local[q] = loc[0] | (loc[1] << 16);
+      }
+    }
+    if (!small.empty()) out.jb_body_start.push_back((uint32_t)out.jb_bodies.size());
+  }
+  // the large components: greedy colouring in arena order
+  std::vector<uint32_t> colour(large.size(), 0);
+  uint32_t n_colours = 0;
+  {
+    std::vector<std::vector<uint32_t>> used(large.empty() ? 0 : nb);
+    for (size_t i = 0; i < large.size(); ++i) {
+      const uint32_t a = ja[large[i]], b = jb[large[i]];
+      uint32_t k = 0;
+      while (std::find(used[a].begin(), used[a].end(), k) != used[a].end() ||
+             std::find(used[b].begin(), used[b].end(), k) != used[b].end())
+        ++k;
+      colour[i] = k;
+      used[a].push_back(k);
+      used[b].push_back(k);
+      n_colours = std::max(n_colours, k + 1);
+    }
+  }
+  out.colour_offsets.assign(n_colours + 1, n_small);
+  for (size_t i = 0; i < large.size(); ++i) out.colour_offsets[colour[i] + 1]++;
+  for (uint32_t k = 0; k < n_colours; ++k) out.colour_offsets[k + 1] += out.colour_offsets[k] - n_small;
+  {
+    std::vector<uint32_t> fill(out.colour_offsets.begin(), out.colour_offsets.end() - 1);
+    for (size_t i = 0; i < large.size(); ++i) out.joint_order[fill[colour[i]]++] = large[i];
+  }
+  return BLOBS_OK;
+}
+
 int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scene& s, HostScene& h) {
   const uint32_t nw = s.n_worlds ? s.n_worlds : 1;
   const uint32_t nb = s.n_bodies, nc = s.n_colliders, ns = s.n_springs, nj = s.n_joints;
@@ -406,154 +570,24 @@ int build_host_scene(const blobs_config& cfg, float cell_scale, const blobs_scen
     }
   }
 
-  // joints: the bodies a chain of joints links form a component, and the
-  // joints of one component touch no body of another, so each component can
-  // be swept on its own -- every iteration, its joints in arena order --
-  // giving each body the reference's sequence of updates (physics.rs:428-431).
-  // Components of at most JB_MAX_JOINTS joints become one thread each of
-  // k_joint_blocks (shared memory, reference order); the joints of larger
-  // ones are greedily coloured in arena order and swept colour by colour.
-  // Processing order: small components block by block, then the large
-  // components' joints by (colour, arena index).
-  std::vector<uint32_t> uf(nb);
-  for (uint32_t i = 0; i < nb; ++i) uf[i] = i;
-  auto find = [&](uint32_t x) {
-    while (uf[x] != x) x = uf[x] = uf[uf[x]];
-    return x;
-  };
   for (uint32_t j = 0; j < nj; ++j) {
     const uint32_t a = s.jnt_a[j], b = s.jnt_b[j];
     if (a >= nb || b >= nb || a == b) return BLOBS_ERR_INVALID_ARGUMENT;
     if (h.body_world[a] != h.body_world[b]) return BLOBS_ERR_INVALID_ARGUMENT;
     if (nw > 1 && (uint32_t)world_of(s.world_joint_offsets, nw, j) != h.body_world[a])
       return BLOBS_ERR_INVALID_ARGUMENT;
-    const uint32_t ra = find(a), rb = find(b);
-    if (ra != rb) uf[std::max(ra, rb)] = std::min(ra, rb);
   }
-  std::vector<uint32_t> comp_joints(nj ? nb : 0, 0), comp_first(nj ? nb : 0, 0xffffffffu);
-  for (uint32_t j = 0; j < nj; ++j) {
-    const uint32_t r = find(s.jnt_a[j]);
-    if (comp_joints[r]++ == 0) comp_first[r] = j;
-  }
-  std::vector<uint32_t> small;  // roots of the small components, in processing order
-  for (uint32_t r = 0; r < (nj ? nb : 0); ++r)
-    if (comp_joints[r] && comp_joints[r] <= JB_MAX_JOINTS) small.push_back(r);
-  std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
-    return comp_joints[x] != comp_joints[y] ? comp_joints[x] > comp_joints[y] : comp_first[x] < comp_first[y];
-  });
-  // Deal the components, largest first, over the blocks in snake order, so
-  // that the largest (the longest sequential sweeps) land in different blocks
-  // and every block gets a similar share of the work; inside a block they stay
-  // largest first.  A component of n joints has at most n + 1 bodies.
-  std::vector<uint32_t> block_first(1, 0);  // component index at which each block starts (in `small`)
-  if (!small.empty()) {
-    uint64_t tot_j = 0;
-    for (uint32_t r : small) tot_j += comp_joints[r];
-    uint64_t nblk = std::max<uint64_t>({(small.size() + JB_THREADS - 1) / JB_THREADS,
-                                        (tot_j * 4 + 3 * JB_JOINTS - 1) / (3 * JB_JOINTS),
-                                        ((tot_j + small.size()) * 4 + 3 * JB_BODIES - 1) / (3 * JB_BODIES), 1});
-    std::vector<std::vector<uint32_t>> dealt;
-    while (true) {
-      nblk = std::min<uint64_t>(nblk, small.size());
-      dealt.assign(nblk, {});
-      std::vector<uint32_t> nj_in(nblk, 0), nb_in(nblk, 0);
-      bool fits = true;
-      for (size_t i = 0; i < small.size() && fits; ++i) {
-        const uint64_t round = i / nblk, pos = i % nblk;
-        uint64_t k = (round & 1) ? nblk - 1 - pos : pos;
-        const uint32_t cj = comp_joints[small[i]];
-        uint64_t tries = 0;
-        while (dealt[k].size() == (size_t)JB_THREADS || nj_in[k] + cj > JB_JOINTS || nb_in[k] + cj + 1 > JB_BODIES) {
-          k = (k + 1) % nblk;
-          if (++tries == nblk) {
-            fits = false;
-            break;
-          }
-        }
-        if (!fits) break;
-        dealt[k].push_back(small[i]);
-        nj_in[k] += cj;
-        nb_in[k] += cj + 1;
-      }
-      if (fits) break;
-      nblk += nblk / 8 + 1;
-    }
-    small.clear();
-    for (const auto& d : dealt) {
-      small.insert(small.end(), d.begin(), d.end());
-      block_first.push_back((uint32_t)small.size());
-    }
-  }
-  std::vector<uint32_t> comp_index(nj ? nb : 0, 0xffffffffu);
-  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) comp_index[small[c]] = c;
-  h.jb_joint_start.assign(small.size() + 1, 0);
-  for (uint32_t c = 0; c < (uint32_t)small.size(); ++c)
-    h.jb_joint_start[c + 1] = h.jb_joint_start[c] + comp_joints[small[c]];
-  const uint32_t n_small = small.empty() ? 0u : h.jb_joint_start.back();
-  h.joint_order.assign(nj, 0);
-  std::vector<uint32_t> large;  // the large components' joints, arena order
   {
-    std::vector<uint32_t> fill(h.jb_joint_start.begin(), h.jb_joint_start.end() - (small.empty() ? 0 : 1));
-    for (uint32_t j = 0; j < nj; ++j) {
-      const uint32_t c = comp_index[find(s.jnt_a[j])];
-      if (c != 0xffffffffu) h.joint_order[fill[c]++] = j;
-      else large.push_back(j);
-    }
-  }
-  // the blocks' bodies, each with its block-local slot
-  h.jb_comp_start.assign(block_first.begin(), block_first.end());
-  h.jb_body_start.assign(1, 0);
-  h.jb_bodies.clear();
-  h.jnt_local.assign(nj, 0);
-  {
-    std::vector<int32_t> slot(nj ? nb : 0, -1);
-    size_t blk = 0;
-    for (uint32_t c = 0; c < (uint32_t)small.size(); ++c) {
-      if (c == block_first[blk + 1]) {
-        for (uint32_t i = h.jb_body_start.back(); i < (uint32_t)h.jb_bodies.size(); ++i) slot[h.jb_bodies[i]] = -1;
-        h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
-        ++blk;
-      }
-      const uint32_t q0 = h.jb_joint_start[c], q1 = h.jb_joint_start[c + 1];
-      for (uint32_t q = q0; q < q1; ++q) {
-        const uint32_t j = h.joint_order[q];
-        uint32_t loc[2];
-        const uint32_t ends[2] = {s.jnt_a[j], s.jnt_b[j]};
-        for (int e2 = 0; e2 < 2; ++e2) {
-          if (slot[ends[e2]] < 0) {
-            slot[ends[e2]] = (int32_t)((uint32_t)h.jb_bodies.size() - h.jb_body_start.back());
-            h.jb_bodies.push_back(ends[e2]);
-          }
-          loc[e2] = (uint32_t)slot[ends[e2]];
-        }
-        h.jnt_local[q] = loc[0] | (loc[1] << 16);
-      }
-    }
-    if (!small.empty()) h.jb_body_start.push_back((uint32_t)h.jb_bodies.size());
-  }
-  // the large components: greedy colouring in arena order
-  std::vector<uint32_t> colour(large.size(), 0);
-  uint32_t n_colours = 0;
-  {
-    std::vector<std::vector<uint32_t>> used(large.empty() ? 0 : nb);
-    for (size_t i = 0; i < large.size(); ++i) {
-      const uint32_t a = s.jnt_a[large[i]], b = s.jnt_b[large[i]];
-      uint32_t k = 0;
-      while (std::find(used[a].begin(), used[a].end(), k) != used[a].end() ||
-             std::find(used[b].begin(), used[b].end(), k) != used[b].end())
-        ++k;
-      colour[i] = k;
-      used[a].push_back(k);
-      used[b].push_back(k);
-      n_colours = std::max(n_colours, k + 1);
-    }
-  }
-  h.colour_offsets.assign(n_colours + 1, n_small);
-  for (size_t i = 0; i < large.size(); ++i) h.colour_offsets[colour[i] + 1]++;
-  for (uint32_t k = 0; k < n_colours; ++k) h.colour_offsets[k + 1] += h.colour_offsets[k] - n_small;
-  {
-    std::vector<uint32_t> fill(h.colour_offsets.begin(), h.colour_offsets.end() - 1);
-    for (size_t i = 0; i < large.size(); ++i) h.joint_order[fill[colour[i]]++] = large[i];
+    JointSchedule js;
+    const int st = joint_schedule(nb, nj, s.jnt_a, s.jnt_b, js);
+    if (st) return st;
+    h.joint_order = std::move(js.joint_order);
+    h.colour_offsets = std::move(js.colour_offsets);
+    h.jb_comp_start = std::move(js.jb_comp_start);
+    h.jb_joint_start = std::move(js.jb_joint_start);
+    h.jb_body_start = std::move(js.jb_body_start);
+    h.jb_bodies = std::move(js.jb_bodies);
+    h.jnt_local = std::move(js.jnt_local);
   }
   h.jnt_a.resize(nj);
   h.jnt_b.resize(nj);
@@ -1384,6 +1418,25 @@ int blobs_world_time(blobs_world* w, double* time, double* accumulator) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
   if (time) *time = w->time;
   if (accumulator) *accumulator = w->accumulator;
+  return BLOBS_OK;
+}
+
+int blobs_joint_schedule(uint32_t n_bodies, uint32_t n_joints, const uint32_t* jnt_a, const uint32_t* jnt_b,
+                         uint32_t* order, uint32_t* block_joint_start, uint32_t* n_blocks, uint32_t* colour_start,
+                         uint32_t* n_colours) {
+  if (n_joints && (!jnt_a || !jnt_b)) return BLOBS_ERR_INVALID_ARGUMENT;
+  JointSchedule js;
+  const int st = joint_schedule(n_bodies, n_joints, jnt_a, jnt_b, js);
+  if (st) return st;
+  const uint32_t nblk = js.jb_comp_start.empty() ? 0u : (uint32_t)js.jb_comp_start.size() - 1u;
+  const uint32_t ncol = js.colour_offsets.empty() ? 0u : (uint32_t)js.colour_offsets.size() - 1u;
+  if (order && n_joints) std::memcpy(order, js.joint_order.data(), sizeof(uint32_t) * n_joints);
+  if (block_joint_start)
+    for (uint32_t k = 0; k <= nblk; ++k) block_joint_start[k] = js.jb_joint_start[js.jb_comp_start[k]];
+  if (n_blocks) *n_blocks = nblk;
+  if (colour_start)
+    for (uint32_t k = 0; k <= ncol; ++k) colour_start[k] = js.colour_offsets[k];
+  if (n_colours) *n_colours = ncol;
   return BLOBS_OK;
 }
 

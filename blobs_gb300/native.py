@@ -94,6 +94,7 @@ def lib() -> ctypes.CDLL:
         "blobs_world_pushout_count": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_time": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "blobs_world_joint_order": (i32, [_P, _P, ctypes.POINTER(u32)]),
+        "blobs_joint_schedule": (i32, [u32, u32, _P, _P, _P, _P, ctypes.POINTER(u32), _P, ctypes.POINTER(u32)]),
         "blobs_body_mass_inertia": (i32, [u32, u32, _P, _P, _P, _P, _P, _P, _P]),
         "blobs_world_set_stream": (i32, [_P, _P]),
         "blobs_world_write_bodies": (i32, [_P, _P, _P, _P, _P, _P]),
@@ -150,6 +151,23 @@ def mass_inertia(scene: scenes.Scene):
                                         _ptr(np.ascontiguousarray(scene.col_sensor, np.uint8)),
                                         _ptr(m), _ptr(I)), "blobs_body_mass_inertia")
     return m, I
+
+
+def joint_schedule(n_bodies: int, jnt_a, jnt_b):
+    """The GPU's joint processing schedule for a joint list, computed on the
+    host (blobs_joint_schedule): (order, block_joint_start, colour_start) --
+    block k sweeps order[block_joint_start[k]:block_joint_start[k+1]], colour k
+    is order[colour_start[k]:colour_start[k+1]]."""
+    a = np.ascontiguousarray(np.asarray(jnt_a, np.uint32))
+    b = np.ascontiguousarray(np.asarray(jnt_b, np.uint32))
+    n = len(a)
+    order = np.zeros(max(1, n), np.uint32)
+    blocks = np.zeros(n + 1, np.uint32)
+    colours = np.zeros(n + 1, np.uint32)
+    nblk, ncol = ctypes.c_uint32(), ctypes.c_uint32()
+    check(lib().blobs_joint_schedule(int(n_bodies), n, _ptr(a), _ptr(b), _ptr(order), _ptr(blocks),
+                                     ctypes.byref(nblk), _ptr(colours), ctypes.byref(ncol)), "joint_schedule")
+    return order[:n], blocks[:nblk.value + 1], colours[:ncol.value + 1]
 
 
 def make_config(scene: Optional[scenes.Scene] = None, *, cell_size: float = 0.0, device: int = 0) -> Config:

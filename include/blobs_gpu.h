@@ -234,6 +234,15 @@ int blobs_world_time(blobs_world* w, double* time, double* accumulator);
  * `order` holds n_joints entries; `n_colours` counts the large components'
  * colours (0 when every component is small). */
 int blobs_world_joint_order(blobs_world* w, uint32_t* order, uint32_t* n_colours);
+/* The same schedule computed on the host for a joint list alone (no device):
+ * `order` (n_joints) as above; block k of the small components sweeps
+ * order[block_joint_start[k] .. block_joint_start[k+1]) (n_blocks + 1 entries,
+ * at most n_joints + 1); colour k of the large components is
+ * order[colour_start[k] .. colour_start[k+1]) (n_colours + 1 entries, at most
+ * n_joints + 1).  Output pointers may be NULL. */
+int blobs_joint_schedule(uint32_t n_bodies, uint32_t n_joints, const uint32_t* jnt_a, const uint32_t* jnt_b,
+                         uint32_t* order, uint32_t* block_joint_start, uint32_t* n_blocks, uint32_t* colour_start,
+                         uint32_t* n_colours);
 
 /* ---- differentiable rollout (no counterpart in the reference) ---------------- */
 
