@@ -129,6 +129,20 @@ struct blobs_world {
   uint32_t cur = 0;
   float2* pos[2] = {nullptr, nullptr};
   void* arena = nullptr;
+  size_t arena_bytes = 0;
+  // blobs_world_snapshot: a copy of the whole device arena (every array of
+  // the loaded scene, its cell tables and counters) and the host-side step
+  // bookkeeping that goes with it
+  struct Snapshot {
+    void* mem = nullptr;
+    size_t bytes = 0;
+    bool valid = false;
+    float old_dt = 1.0f, v_div = 0.0f;
+    double time = 0.0, accumulator = 0.0;
+    uint32_t cur = 0, sticky_status = 0;
+    int vbuf = 0;
+    bool pending = false, keys_valid = false;
+  } snap;
   Counters* dcounters = nullptr;
   Counters* hcounters = nullptr;  // pinned
   WorldDev dev{};
@@ -202,9 +216,14 @@ struct blobs_world {
     if (rec.ckpt) cudaFree(rec.ckpt);
     rec = Recording();
   }
+  void drop_snapshot() {
+    if (snap.mem) cudaFree(snap.mem);
+    snap = Snapshot();
+  }
   void release() {
     drop_graphs();
     drop_recording();
+    drop_snapshot();
     if (ev_mem) cudaFree(ev_mem);
     ev_mem = nullptr;
     events_on = false;
@@ -1150,8 +1169,10 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   cudaStreamSynchronize(w->st());
   w->drop_graphs();
   w->drop_recording();
+  w->drop_snapshot();
   if (w->arena) cudaFree(w->arena);
   w->arena = nullptr;
+  w->arena_bytes = 0;
   w->loaded = false;
 
   const uint32_t nb = scene->n_bodies, nc = scene->n_colliders, ns = scene->n_springs, nj = scene->n_joints;
@@ -1180,6 +1201,7 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   carve(sizer, d, w->pos, &counters, h, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
   e = cudaMalloc(&w->arena, sizer.off + 256);
   if (e != cudaSuccess) return blobs_map_cuda(e);
+  w->arena_bytes = sizer.off + 256;
   Carver cv;
   cv.base = static_cast<char*>(w->arena);
   carve(cv, d, w->pos, &counters, h, nb, nc, ns, nj, nw, ncirc, h.n_cells, n_tiles, sorted_storage);
@@ -1437,6 +1459,55 @@ int blobs_joint_schedule(uint32_t n_bodies, uint32_t n_joints, const uint32_t* j
   if (colour_start)
     for (uint32_t k = 0; k <= ncol; ++k) colour_start[k] = js.colour_offsets[k];
   if (n_colours) *n_colours = ncol;
+  return BLOBS_OK;
+}
+
+int blobs_world_snapshot(blobs_world* w) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  if (w->snap.bytes != w->arena_bytes) {
+    w->drop_snapshot();
+    e = cudaMalloc(&w->snap.mem, w->arena_bytes);
+    if (e != cudaSuccess) {
+      w->snap = blobs_world::Snapshot();
+      return blobs_map_cuda(e);
+    }
+    w->snap.bytes = w->arena_bytes;
+  }
+  e = cudaMemcpyAsync(w->snap.mem, w->arena, w->arena_bytes, cudaMemcpyDeviceToDevice, w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  w->snap.valid = true;
+  w->snap.old_dt = w->old_dt;
+  w->snap.v_div = w->v_div;
+  w->snap.time = w->time;
+  w->snap.accumulator = w->accumulator;
+  w->snap.cur = w->cur;
+  w->snap.sticky_status = w->sticky_status;
+  w->snap.vbuf = w->vbuf;
+  w->snap.pending = w->pending;
+  w->snap.keys_valid = w->keys_valid;
+  return BLOBS_OK;
+}
+
+int blobs_world_restore(blobs_world* w) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded || !w->snap.valid || w->snap.bytes != w->arena_bytes) return BLOBS_ERR_STATE;
+  cudaError_t e = cudaSetDevice(w->cfg.device);
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  e = cudaMemcpyAsync(w->arena, w->snap.mem, w->arena_bytes, cudaMemcpyDeviceToDevice, w->st());
+  if (e != cudaSuccess) return blobs_map_cuda(e);
+  w->old_dt = w->snap.old_dt;
+  w->v_div = w->snap.v_div;
+  w->time = w->snap.time;
+  w->accumulator = w->snap.accumulator;
+  w->cur = w->snap.cur;
+  w->sticky_status = w->snap.sticky_status;
+  w->vbuf = w->snap.vbuf;
+  w->pending = w->snap.pending;
+  w->keys_valid = w->snap.keys_valid;
+  w->drop_recording();  // a recorded rollout belongs to the trajectory it recorded
   return BLOBS_OK;
 }
 

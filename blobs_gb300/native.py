@@ -94,6 +94,8 @@ def lib() -> ctypes.CDLL:
         "blobs_world_pushout_count": (i32, [_P, ctypes.POINTER(u64)]),
         "blobs_world_time": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "blobs_world_joint_order": (i32, [_P, _P, ctypes.POINTER(u32)]),
+        "blobs_world_snapshot": (i32, [_P]),
+        "blobs_world_restore": (i32, [_P]),
         "blobs_joint_schedule": (i32, [u32, u32, _P, _P, _P, _P, ctypes.POINTER(u32), _P, ctypes.POINTER(u32)]),
         "blobs_body_mass_inertia": (i32, [u32, u32, _P, _P, _P, _P, _P, _P, _P]),
         "blobs_world_set_stream": (i32, [_P, _P]),
@@ -431,6 +433,14 @@ class World:
         t, a = ctypes.c_double(), ctypes.c_double()
         check(lib().blobs_world_time(self._h, ctypes.byref(t), ctypes.byref(a)), "time")
         return t.value, a.value
+
+    def snapshot(self) -> None:
+        """Keep the world's whole state (blobs_world_snapshot)."""
+        check(lib().blobs_world_snapshot(self._h), "snapshot")
+
+    def restore(self) -> None:
+        """Back to the state of the last snapshot (blobs_world_restore)."""
+        check(lib().blobs_world_restore(self._h), "restore")
 
     def joint_order(self):
         order = np.zeros(max(1, self.n_joints), np.uint32)

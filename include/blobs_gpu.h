@@ -182,6 +182,20 @@ int blobs_world_set_stream(blobs_world* w, void* stream);
 int blobs_world_write_bodies(blobs_world* w, const float* pos, const float* pos_old, const float* vel,
                              const float* rotation, const float* angvel);
 
+/* ---- snapshot / restore (no reference counterpart) -------------------------- */
+
+/* Copy the world's whole device state -- every array of the loaded scene
+ * (positions, previous positions, velocities, rotations, collider snapshots,
+ * pending velocity requests, cell tables, contact counters) -- and its step
+ * bookkeeping (old_dt, time, fixed-step accumulator) into a snapshot the
+ * world holds (one per world, device memory the size of the scene), and
+ * restore it: stepping after a restore repeats the steps taken after the
+ * snapshot bit for bit.  Device-to-device and asynchronous on the world's
+ * stream.  Loading a scene drops the snapshot; restoring drops a recorded
+ * rollout; the collision-event buffer is not part of the state. */
+int blobs_world_snapshot(blobs_world* w);
+int blobs_world_restore(blobs_world* w);
+
 /* ---- per-phase device timing (profiling aid; no reference counterpart) ------ */
 
 /* Number of kernels this world has issued (eagerly or as nodes of a launched
