@@ -23,7 +23,7 @@ enum : uint8_t {
 // Device status bits, read back by the host after a synchronising call.
 enum : uint32_t {
   ST_NAN = 1u,         // NaN contact normal or non-finite rotation (physics.rs:293, 471-474)
-  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (no kernel of this build waits on another)
+  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (reserved: no kernel waits on another)
   ST_BAD_INDEX = 4u,   // a device bounds check fired
 };
 

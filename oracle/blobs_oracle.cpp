@@ -1,7 +1,7 @@
 // blobs_oracle.cpp -- TEST INFRASTRUCTURE, NOT THE PRODUCT.
 //
 // A CPU restatement of the reference `Physics::step` of darthdeus/blobs
-// (Rust, blobs 0.2.1), used only as the checker by tests/, by
+// (Rust, blobs 0.2.1), used only to check results, by tests/, by
 // __graft_entry__.smoke() and by bench.py's CPU-baseline leg.  Nothing in the
 // shipped library links or calls this file.
 //

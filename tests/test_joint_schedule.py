@@ -65,7 +65,7 @@ def check_schedule(n_bodies, a, b):
     return order, blocks, colours
 
 
-def test_configuration_3_joints():
+def test_jointed_world_joints():
     s = scenes.jointed_bodies(seed=3, n=20000, n_joints=5000, n_springs=0, side=475.0)
     order, blocks, colours = check_schedule(s.n_bodies, s.jnt_a, s.jnt_b)
     assert len(colours) <= 1  # all components small

@@ -152,9 +152,10 @@ def test_static_kinematic_bodies_sensors_groups_bit_exact():
 
 
 def test_multi_collider_bodies_bit_exact():
-    """Config 3 layout without joints: rotation stays 0, so the snapshots
-    (rot(0) * offset + p) are exact and the merged per-body contact order is
-    the reference's (outer collider, inner collider) sequence."""
+    """The jointed-world layout (1-4 colliders per body) without joints:
+    rotation stays 0, so the snapshots (rot(0) * offset + p) are exact and
+    the merged per-body contact order is the reference's (outer collider,
+    inner collider) sequence."""
     s = scenes.jointed_bodies(seed=3, n=6000, n_joints=0, n_springs=2000, side=90.0)
     s.jnt_a = s.jnt_a[:0]
     got, want = run_gpu(s, 4), run_oracle(s, 4)

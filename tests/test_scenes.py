@@ -1,6 +1,6 @@
-"""The seeded workload generators against the benchmark configurations they
-stand for (no dataset exists; these are synthetic scenes with the
-configurations' shapes, sizes and distributions).  No GPU."""
+"""The seeded workload generators against the workloads they stand for (no
+dataset exists; these are synthetic scenes with the stated shapes, sizes and
+distributions).  No GPU."""
 import math
 
 import numpy as np
@@ -13,7 +13,7 @@ def packing(s):
     return area / float(np.prod(s.world_box[0, 2:] - s.world_box[0, :2]))
 
 
-def test_sparse_spheres_configuration_1():
+def test_sparse_spheres_1000_in_a_40_box():
     s = scenes.sparse_spheres()
     assert s.n_bodies == 1000 and s.single_collider() and s.dt == 1.0 / 60.0 and s.n_steps == 600
     assert s.col_radius.min() >= 0.1 and s.col_radius.max() <= 0.3
@@ -25,7 +25,7 @@ def test_sparse_spheres_configuration_1():
     assert abs(float(s.vreq.std()) - 1.0) < 0.1 and s.vreq_set.all()
 
 
-def test_dense_spheres_configuration_2():
+def test_dense_spheres_at_40_percent_packing():
     s = scenes.dense_spheres(n=200_000)  # the same generator as the 1M-sphere world, smaller
     assert s.dt == 1.0 / 120.0 and s.single_collider()
     assert 0.05 <= s.col_radius.min() and s.col_radius.max() <= 0.15
@@ -36,7 +36,7 @@ def test_dense_spheres_configuration_2():
     assert abs(scenes.box_side(1_000_000, 0.05, 0.15, 0.40) - 291.7) < 0.1
 
 
-def test_jointed_bodies_configuration_3():
+def test_jointed_bodies_colliders_joints_springs():
     s = scenes.jointed_bodies(n=20000, n_joints=5000, n_springs=10000, side=475.0)
     per_body = np.bincount(s.col_parent, minlength=s.n_bodies)
     assert per_body.min() == 1 and per_body.max() == 4
@@ -53,7 +53,7 @@ def test_jointed_bodies_configuration_3():
     assert s.dt == 1.0 / 120.0
 
 
-def test_uneven_batch_configuration_4():
+def test_uneven_batch_log_uniform_worlds():
     s = scenes.uneven_batch(n_worlds=256)
     counts = np.diff(s.world_body_offsets)
     assert s.n_worlds == 256 and counts.min() >= 64 and counts.max() <= 8192
@@ -70,7 +70,7 @@ def test_uneven_batch_configuration_4():
         assert abs(sub.n_springs - 0.1 * sub.n_bodies) <= 1
 
 
-def test_gradient_batch_configuration_5():
+def test_gradient_batch_256_worlds_of_2048():
     s, marked, targets = scenes.gradient_batch(n_worlds=4)
     assert s.n_worlds == 4 and s.n_bodies == 4 * 2048 and s.n_springs == 4 * 1024
     assert s.dt == 1.0 / 60.0 and s.n_steps == 120
