@@ -68,3 +68,19 @@ def test_world_create_without_device_is_an_error_not_a_fallback():
         native.lib().blobs_world_destroy(h)
     else:
         assert st == native.ERR_NO_DEVICE
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/blobs_gpu.h compiles as C99 (no C++ types cross the boundary),
+    and a C program can take the address of every entry point."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    refs = "\n".join("  (void (*)(void))&%s," % n for n in declared_symbols())
+    src.write_text('#include "blobs_gpu.h"\nvoid (*entry_points[])(void) = {\n%s\n};\n' % refs)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
