@@ -86,3 +86,17 @@ def test_generators_are_seeded():
     assert np.array_equal(a.pos, b.pos) and np.array_equal(a.col_radius, b.col_radius)
     c = scenes.dense_spheres(seed=8, n=5000)
     assert not np.array_equal(a.pos, c.pos)
+
+
+def test_pack_and_unpack_round_trip():
+    rng = np.random.Generator(np.random.PCG64(12))
+    worlds = [scenes.random_world(rng, n, 0.1, 0.3, 0.35, 1.0, spring_frac=0.2) for n in (50, 300, 120)]
+    packed = scenes.pack(worlds)
+    assert packed.n_worlds == 3 and packed.n_bodies == 470
+    for k, w in enumerate(worlds):
+        u = scenes.unpack_world(packed, k)
+        for name in ("pos", "vreq", "col_radius", "col_offset", "spr_rest", "spr_k", "spr_c"):
+            assert np.array_equal(getattr(u, name), getattr(w, name)), (k, name)
+        assert np.array_equal(u.col_parent, w.col_parent) and np.array_equal(u.spr_a, w.spr_a)
+        assert np.array_equal(u.spr_b, w.spr_b)
+        assert np.array_equal(u.world_box[0], w.world_box[0])
