@@ -5,7 +5,8 @@ the reference's C^2/2 loop, pinned to it in tests/test_oracle_grid.py) makes
 the full scenes checkable in seconds:
 
 * 1,000,000 spheres, r ~ U[0.05, 0.15], 40% packing with overlaps, dt = 1/120
-  (the benchmark world): five steps, bit-exact.
+  (the benchmark world): five steps, bit-exact; one step within the stated
+  tolerance of the f64 re-run.
 * 4,096 uneven worlds, 64..8,192 bodies each (7.0M bodies), springs on 10%:
   one batched step, bit-exact world by world.
 * 256 worlds x 2,048 spheres with 1,024 springs each (the differentiable
@@ -59,6 +60,23 @@ def test_million_spheres_five_steps_bit_exact():
     assert want["contacts"] > 9_000_000
     assert got["contacts"] == want["contacts"]
     assert_exact(got, want, ("pos", "pos_old", "vel", "snap"))
+
+
+def test_million_spheres_one_step_within_f64_tolerance():
+    """The stated single-step tolerance against an f64 re-run of the same
+    step, at full size: 99% of position components within 1e-4 (1 + |x|) of
+    f64 (measured: 99.92%), and no position or velocity component further
+    from f64 than the f32 reference's own largest deviation -- the
+    overlapping start amplifies f32 rounding at contact-threshold flips in
+    the reference algorithm itself, and velocities (the last substep's
+    displacement over dt = 1/960) amplify it 960-fold."""
+    s = scenes.dense_spheres(seed=2, n=1_000_000)
+    got, want, ref32 = gpu_run(s, 1), oracle_run(s, 1, 64), oracle_run(s, 1, 32)
+    err = np.abs(got["pos"].astype(np.float64) - want["pos"])
+    assert np.mean(err <= 1e-4 * (1.0 + np.abs(want["pos"]))) >= 0.99
+    for k in ("pos", "vel"):
+        err = np.abs(got[k].astype(np.float64) - want[k])
+        assert err.max() <= np.abs(ref32[k] - want[k]).max() * (1.0 + 1e-6), k
 
 
 def check_batched(scene, got, steps):
