@@ -179,15 +179,13 @@ __device__ __host__ __forceinline__ int32_t cell_coord(float v, float cs) {
   return (int32_t)q;
 }
 
-// Cell coordinate of the broadphase grid: floor(v * (1/cs)), saturating,
-// NaN -> 0.  Monotone in v; with cs >= 2 rmax (1 + 1/64) two spheres in
-// contact always land in 3x3-neighbouring cells for |v| / cs up to ~1e5.
-__device__ __host__ __forceinline__ int32_t grid_coord(float v, float inv_cs) {
+// floor(q) as int32, saturating, NaN -> 0.
+__device__ __host__ __forceinline__ int32_t floor_sat(float q) {
 #ifdef __CUDA_ARCH__
   // cvt.rmi.s32.f32: floor, saturating, NaN -> 0 -- the same function
-  return __float2int_rd(v * inv_cs);
+  return __float2int_rd(q);
 #else
-  float q = floorf(v * inv_cs);
+  q = floorf(q);
   if (q != q) return 0;
   if (q >= 2147483648.0f) return 2147483647;
   if (q <= -2147483648.0f) return (-2147483647 - 1);
@@ -195,11 +193,49 @@ __device__ __host__ __forceinline__ int32_t grid_coord(float v, float inv_cs) {
 #endif
 }
 
+// Below this many cells from the grid origin the plain f32 formula is used.
+constexpr float GRID_FAST_CELLS = 32768.0f;
+
+// floor((v - o) * inv) in real arithmetic, for |v - o| * inv at or beyond
+// GRID_FAST_CELLS: the difference is carried exactly as s + e (TwoSum), the
+// product s * inv exactly as p + r1 (an FMA residual, exact in f32), so the
+// result is within ~|X| 2^-46 cells of the real-number floor for every
+// |X| < 2^31 (saturating beyond, which merges cells and stays exact).
+__device__ __host__ __noinline__ inline int32_t grid_coord_far(float v, float o, float inv) {
+  const float s = v - o;
+  const float bb = s - v;
+  const float e = (v - (s - bb)) + ((-o) - bb);
+  const float p = s * inv;
+  const float r1 = fmaf(s, inv, -p);
+  const float t = r1 + e * inv;
+  const float fl = floorf(p);
+  float fg = floorf((p - fl) + t);  // p - floor(p) is exact
+  fg = fminf(fmaxf(fg, -1024.0f), 1024.0f);
+  const float flc = fminf(fmaxf(fl, -4.0e18f), 4.0e18f);  // saturate after the sum, in 64 bits
+  const long long k = (long long)flc + (long long)fg;
+  return k > 2147483647ll ? 2147483647 : (k < -2147483648ll ? (int32_t)(-2147483647 - 1) : (int32_t)k);
+}
+
+// Cell coordinate of the broadphase grid: floor((v - o) * inv), saturating,
+// NaN -> 0, monotone in v.  With cs >= 2 rmax (1 + 1/64) and inv = fl(1/cs)
+// two spheres in contact under the reference's own f32 test
+// (sqrt(d.d) < ra + rb) are less than 0.985 of a grid cell apart; the
+// plain formula fl(fl(v - o) * inv) is off by at most 2^-8 of a cell below
+// GRID_FAST_CELLS cells from the origin, and grid_coord_far is off by a
+// negligible amount above it, so such spheres always land in
+// 3x3-neighbouring cells, however far from the origin they are.
+__device__ __host__ __forceinline__ int32_t grid_coord(float v, float o, float inv) {
+  const float q = (v - o) * inv;
+  const float aq = fabsf(q);
+  if (aq < GRID_FAST_CELLS || !(aq <= 3.402823466e38f)) return floor_sat(q);  // NaN, +-inf: saturate
+  return grid_coord_far(v, o, inv);
+}
+
 // Global cell index of a point in world `wp`'s toroidal grid:
 // cell = floor((v - origin) * (1/cs)) wrapped mod the grid size.
 __device__ __host__ __forceinline__ uint32_t cell_key(const WorldParam& wp, float2 s) {
-  uint32_t ix = (uint32_t)grid_coord(s.x - wp.ox, wp.inv_cs) & ((1u << wp.log2w) - 1u);
-  uint32_t iy = (uint32_t)grid_coord(s.y - wp.oy, wp.inv_cs) & ((1u << wp.log2h) - 1u);
+  uint32_t ix = (uint32_t)grid_coord(s.x, wp.ox, wp.inv_cs) & ((1u << wp.log2w) - 1u);
+  uint32_t iy = (uint32_t)grid_coord(s.y, wp.oy, wp.inv_cs) & ((1u << wp.log2h) - 1u);
   return wp.cell_base + ((iy << wp.log2w) | ix);
 }
 

@@ -293,7 +293,7 @@ __device__ __forceinline__ void integrate_body(const WorldDev& w, uint32_t b, fl
 template <class F>
 __device__ __forceinline__ void for_each_candidate(const WorldDev& w, const WorldParam& wp, float2 s, F&& f) {
   const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
-  const uint32_t ix = (uint32_t)grid_coord(s.x - wp.ox, wp.inv_cs), iy = (uint32_t)grid_coord(s.y - wp.oy, wp.inv_cs);
+  const uint32_t ix = (uint32_t)grid_coord(s.x, wp.ox, wp.inv_cs), iy = (uint32_t)grid_coord(s.y, wp.oy, wp.inv_cs);
   const uint32_t x0 = (ix - 1u) & wm, x2 = (ix + 1u) & wm;
 #pragma unroll 1
   for (int oy = -1; oy <= 1; ++oy) {

@@ -74,7 +74,7 @@ struct Grid {
 // The grid every kernel derives from the header: cell = 2 rmax (1 + 1/64),
 // origin one cell before the extent, power-of-two sides capped to
 // NA_MAX_CELLS cells (coordinates wrap beyond, which keeps the 3x3 search
-// exact).
+// exact; blobs::grid_coord keeps it exact at any distance from the origin).
 __device__ inline Grid grid_of(const uint32_t* hdr) {
   Grid g;
   const float rmax = __uint_as_float(hdr[4]);
@@ -102,8 +102,8 @@ __device__ inline Grid grid_of(const uint32_t* hdr) {
 }
 
 __device__ inline uint32_t key_of(const Grid& g, float x, float y) {
-  const uint32_t ix = (uint32_t)__float2int_rd((x - g.ox) * g.inv) & ((1u << g.log2w) - 1u);
-  const uint32_t iy = (uint32_t)__float2int_rd((y - g.oy) * g.inv) & ((1u << g.log2h) - 1u);
+  const uint32_t ix = (uint32_t)blobs::grid_coord(x, g.ox, g.inv) & ((1u << g.log2w) - 1u);
+  const uint32_t iy = (uint32_t)blobs::grid_coord(y, g.oy, g.inv) & ((1u << g.log2h) - 1u);
   return (iy << g.log2w) | ix;
 }
 
@@ -126,8 +126,10 @@ __global__ void na_bounds(Scratch s, uint32_t n, const float2* __restrict__ snap
     atomicMax(s.hdr + 2, ordered(p.x));
     atomicMax(s.hdr + 3, ordered(p.y));
   }
+  // +inf counts (every collider then shares one cell, as in the world
+  // path); NaN never passes the contact test and is left out
   const float r = radius[i];
-  if (r > 0.0f && isfinite(r)) atomicMax(s.hdr + 4, __float_as_uint(r));
+  if (r > 0.0f) atomicMax(s.hdr + 4, __float_as_uint(r));
 }
 
 __global__ void na_keys(Scratch s, uint32_t n, const float2* __restrict__ snap) {
@@ -194,7 +196,7 @@ __global__ void na_emit(Scratch s, uint32_t n, const uint32_t* __restrict__ pare
   const uint32_t c = __float_as_uint(me.w);
   if (c >= n) return;
   const uint32_t wm = (1u << g.log2w) - 1u, hm = (1u << g.log2h) - 1u;
-  const uint32_t ix = (uint32_t)__float2int_rd((me.x - g.ox) * g.inv), iy = (uint32_t)__float2int_rd((me.y - g.oy) * g.inv);
+  const uint32_t ix = (uint32_t)blobs::grid_coord(me.x, g.ox, g.inv), iy = (uint32_t)blobs::grid_coord(me.y, g.oy, g.inv);
   for (int oy = -1; oy <= 1; ++oy) {
     const uint32_t row = ((iy + (uint32_t)oy) & hm) << g.log2w;
     for (int ox = -1; ox <= 1; ++ox) {

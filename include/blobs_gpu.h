@@ -366,6 +366,9 @@ int blobs_spatial_hash_query(blobs_spatial_hash* h, uint64_t nq, const float* qx
  *   n uint32 (device) or NULL (all different / all groups);
  *   pairs: 2 * cap uint32 (device); count: one device counter that receives
  *   the full number of pairs (pairs past `cap` are counted, not written).
+ * Any finite coordinates are exact (no pair is lost far from the origin); a
+ * non-finite snapshot or a NaN radius gives no pair, a +inf radius a pair
+ * with every collider the filters allow -- as in the world path.
  * Asynchronous on `stream` (a cudaStream_t, NULL = the legacy default).  The
  * first call on a device looks up the device address of the scratch array
  * (once, with that device current); make that first call before any stream

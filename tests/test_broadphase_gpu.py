@@ -6,22 +6,16 @@ import pytest
 
 from blobs_gb300 import native, scenes
 from oracle import oracle
+from tests.gridkey import grid_coord
 
 pytestmark = pytest.mark.gpu
-
-
-def grid_coord(v, inv_cs):
-    """floor(v * inv_cs) in float32, saturating, NaN -> 0 (the grid function)."""
-    q = np.floor(np.asarray(v, np.float32) * np.float32(inv_cs)).astype(np.float64)
-    q = np.where(np.isnan(q), 0.0, q)
-    return np.clip(q, -2 ** 31, 2 ** 31 - 1).astype(np.int64)
 
 
 def cpu_candidates(snap, inv_cs, origin, log2w, log2h):
     """All (hi, lo) pairs whose wrapped cells are 3x3 neighbours."""
     W, H = 1 << log2w, 1 << log2h
-    ix = grid_coord(snap[:, 0].astype(np.float32) - np.float32(origin[0]), inv_cs) % W
-    iy = grid_coord(snap[:, 1].astype(np.float32) - np.float32(origin[1]), inv_cs) % H
+    ix = grid_coord(snap[:, 0].astype(np.float32), origin[0], inv_cs) % W
+    iy = grid_coord(snap[:, 1].astype(np.float32), origin[1], inv_cs) % H
     key = iy * W + ix
     order = np.argsort(key, kind="stable")
     buckets = {}
