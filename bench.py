@@ -1,20 +1,26 @@
 #!/usr/bin/env python3
 """Benchmark of the blobs step on GB300: sphere-steps/s of a 1,000,000-sphere
 world (Physics::step = 8 substeps at dt = 1/120, r ~ U[0.05, 0.15], 40%
-packing with overlaps, walled box, seeded synthetic scene).
+packing with overlaps, walled box, seeded synthetic scene, 1,000-step
+rollout).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --section general|batched [--steps K] [--warmup W]
 
-One JSON line on rank 0.  `value` is device-timed (CUDA events on the
-world's stream, L2 flushed between steps, inputs resident in HBM) over steps
-W .. W+K-1 of the scene; the phase-timing and end-to-end legs reload the
-scene and time the same window.  `e2e` is
-the same metric through the C ABI with the body state written from and read
-back into pinned host memory every step; `roofline` is the dominant kernel's
-algorithmic bytes per launch over its event-timed duration; `cpu_baseline`
-is the oracle (the CPU restatement of the reference step) on bounded samples
-of the same workload, extrapolated with the reference's O(N^2) cost model.
+One JSON line on rank 0.  The whole 1,000-step rollout runs from t = 0,
+every step between its own CUDA-event pair on the world's stream with L2
+flushed before it (inputs resident in HBM); `value` is over K steps evenly
+spaced across steps W .. 999 (a stratified sample of the rollout, whose
+contact load grows along it), `rollout` over all 1,000.  The phase-timing,
+roofline and end-to-end legs reload the scene and time the same K steps.
+`e2e` is the same metric through the C ABI with the body state written from
+and read back into pinned host memory every step; `roofline` is the step
+kernel's algorithmic bytes per launch over its event-timed duration (events
+around that kernel alone); `cpu_baseline` is the oracle (the CPU restatement
+of the reference step) on bounded samples of the same workload, extrapolated
+with the reference's O(N^2) cost model.  Secondary workloads follow: the
+1,000-sphere world in full on GPU and CPU, the 4,096 batched worlds, the
+differentiable batch, the jointed world, the literal 2000 x 2000 box.
 With --gpus N > 1 (torchrun) every rank steps its own independent world
 (replicas; the path has no data exchange).  --section runs one secondary
 workload alone (the 200k-body jointed world, or the 4,096 batched worlds)
@@ -38,6 +44,7 @@ sys.path.insert(0, ROOT)
 # algorithmic bytes (the minimal traffic model of the path)
 BYTES_PER_BODY_SUBSTEP = 56      # state 40 B (read pos, pos_old, radius, mass; write pos, pos_old) + broadphase 16 B
 BYTES_CONTACT_PER_BODY = 48      # fused contact+integrate: state 40 B + read back cell key + index 8 B
+BYTES_PER_SPRING_SUBSTEP = 20    # a, b, rest, k, c
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -153,6 +160,79 @@ def cpu_baseline(sizes=(4096, 8192, 16384, 32768), target_n=1_000_000, seed=2, s
     }
 
 
+def _fit_quadratic(ns, ts):
+    """Least-squares t(N) = a N^2 + b N (the reference's C^2/2 pair loop
+    plus per-body work)."""
+    import numpy as np
+    A = np.array([[n * n, n] for n in ns], float)
+    coef, *_ = np.linalg.lstsq(A, np.array(ts), rcond=None)
+    return float(coef[0]), float(coef[1])
+
+
+def cpu_general(sizes=(2000, 4000, 8000), target_n=200_000, seed=3):
+    """The oracle step on jointed worlds of the same density (side scaled
+    with sqrt(N), joints N/4, springs N/2), fitted and extrapolated to the
+    200k-body world."""
+    from blobs_gb300 import scenes
+    from oracle import oracle
+    ns, ts = [], []
+    for n in sizes:
+        s = scenes.jointed_bodies(seed=seed, n=n, n_joints=n // 4, n_springs=n // 2,
+                                  side=1500.0 * (n / 200_000.0) ** 0.5)
+        w = oracle.OracleWorld(s, 32, maintain_spatial_hash=True)
+        w.time_steps(s.dt, 1)
+        ns.append(n)
+        ts.append(w.time_steps(s.dt, 1))
+    a, b = _fit_quadratic(ns, ts)
+    t = a * target_n * target_n + b * target_n
+    return {"value": target_n / t, "unit": "body-steps/s", "cores": 1, "kind": "port",
+            "sample": "oracle Physics::step on %s-body jointed worlds of the same density (1 step each, %.1f s), "
+                      "fit t = a N^2 + b N, extrapolated to N=%d: %.1f s/step"
+                      % ("/".join(map(str, ns)), sum(ts), target_n, t)}
+
+
+def cpu_batched(scene, sample=48):
+    """The oracle step on `sample` worlds of the uneven batch (evenly spaced
+    by index), fitted t(N) = a N^2 + b N over their body counts and summed
+    over all worlds' body counts: one CPU step of the whole batch."""
+    import numpy as np
+    from blobs_gb300 import scenes
+    from oracle import oracle
+    idx = np.linspace(0, scene.n_worlds - 1, sample).astype(int)
+    ns, ts = [], []
+    for i in idx:
+        sub = scenes.unpack_world(scene, int(i))
+        w = oracle.OracleWorld(sub, 32, maintain_spatial_hash=True)
+        w.time_steps(scene.dt, 1)
+        ns.append(sub.n_bodies)
+        ts.append(w.time_steps(scene.dt, 1))
+    a, b = _fit_quadratic(ns, ts)
+    counts = np.diff(scene.world_body_offsets).astype(np.float64)
+    t = float(np.sum(a * counts * counts + b * counts))
+    return {"value": scene.n_bodies / t, "unit": "sphere-steps/s", "cores": 1, "kind": "port",
+            "sample": "oracle Physics::step on %d evenly spaced worlds (%d-%d bodies, %.1f s), fit t = a N^2 + b N, "
+                      "summed over all %d worlds: %.2f s per batch step"
+                      % (sample, min(ns), max(ns), sum(ts), scene.n_worlds, t)}
+
+
+def cpu_gradient_batch(scene, sample=4):
+    """The oracle forward step on `sample` of the 256 equal worlds, scaled
+    by the world count (the reference has no backward pass)."""
+    import numpy as np
+    from blobs_gb300 import scenes
+    from oracle import oracle
+    ts = []
+    for i in np.linspace(0, scene.n_worlds - 1, sample).astype(int):
+        sub = scenes.unpack_world(scene, int(i))
+        w = oracle.OracleWorld(sub, 32, maintain_spatial_hash=True)
+        w.time_steps(scene.dt, 1)
+        ts.append(w.time_steps(scene.dt, 1))
+    t = float(np.mean(ts)) * scene.n_worlds
+    return {"value": scene.n_bodies / t, "unit": "sphere-steps/s (forward)", "cores": 1, "kind": "port",
+            "sample": "oracle Physics::step (forward) on %d of the %d worlds, mean %.3f s, times %d: %.1f s per "
+                      "batch step" % (sample, scene.n_worlds, float(np.mean(ts)), scene.n_worlds, t)}
+
+
 def max_over_ranks(value, dist, device):
     """The largest `value` over all ranks (the job's time is its slowest
     rank's); `dist` is torch.distributed or None for one process."""
@@ -259,11 +339,12 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def batched_comparison(dev, steps=100, sample=256, seed=4):
-    """4,096 uneven worlds stepped as one batch (a 100-step
-    rollout captured in one CUDA graph) against the per-world form (each
-    world its own device world and its own 100-step rollout launch), timed on
-    `sample` evenly spaced worlds and scaled to all 4,096 by body count."""
+def batched_comparison(dev, steps=100, sample=1024, seed=4):
+    """4,096 uneven worlds stepped as one batch (a 100-step rollout captured
+    in one CUDA graph) against the per-world form (each world its own device
+    world and its own 100-step rollout launch), timed on `sample` evenly
+    spaced worlds -- each created, captured, timed and closed in turn -- and
+    scaled to all 4,096 by body count."""
     import numpy as np
     import torch
     from blobs_gb300 import native, scenes
@@ -284,8 +365,8 @@ def batched_comparison(dev, steps=100, sample=256, seed=4):
     batched_ms = e0.elapsed_time(e1)
     w.sync()
     w.close()
-    idx = np.linspace(0, scene.n_worlds - 1, sample).astype(int)
-    worlds, bodies = [], 0
+    idx = np.unique(np.linspace(0, scene.n_worlds - 1, sample).astype(int))
+    sample_ms, bodies = 0.0, 0
     for i in idx:
         sub = scenes.unpack_world(scene, int(i))
         ww = native.World(sub, device=dev.index)
@@ -293,23 +374,26 @@ def batched_comparison(dev, steps=100, sample=256, seed=4):
         for _ in range(3):
             ww.step(dt)
         ww.rollout(dt, steps)  # capture
-        worlds.append(ww)
-        bodies += sub.n_bodies
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for ww in worlds:
+        torch.cuda.synchronize()
+        e0.record(stream)
         ww.rollout(dt, steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    sample_ms = e0.elapsed_time(e1)
-    for ww in worlds:
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sample_ms += e0.elapsed_time(e1)
+        bodies += sub.n_bodies
         ww.close()
     per_world_ms = sample_ms * scene.n_bodies / bodies
-    return {"worlds": scene.n_worlds, "bodies": scene.n_bodies, "steps": steps,
+    peak, peak_kind = peak_hbm()
+    per_body_substep = BYTES_PER_BODY_SUBSTEP + BYTES_PER_SPRING_SUBSTEP * scene.n_springs / scene.n_bodies
+    achieved = per_body_substep * scene.substeps * scene.n_bodies * steps / (batched_ms / 1e3) / 1e9
+    return {"worlds": scene.n_worlds, "bodies": scene.n_bodies, "springs": scene.n_springs, "steps": steps,
             "batched_ms": batched_ms, "per_world_ms_est": per_world_ms, "speedup": per_world_ms / batched_ms,
             "batched_sphere_steps_per_s": scene.n_bodies * steps / (batched_ms / 1e3),
-            "sample": "%d evenly spaced worlds (%d bodies) run one rollout launch per world, scaled by body count"
-                      % (sample, bodies)}
+            "sample": "%d evenly spaced worlds (%d bodies), one rollout launch per world, scaled by body count"
+                      % (len(idx), bodies),
+            "roofline": {"bound": "hbm", "alg_bytes_per_body_substep": per_body_substep, "achieved": achieved,
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak},
+            "cpu_baseline": cpu_batched(scene)}
 
 
 def general_comparison(dev, steps=10, warmup=3, seed=3):
@@ -342,7 +426,8 @@ def general_comparison(dev, steps=10, warmup=3, seed=3):
     w.close()
     return {"bodies": scene.n_bodies, "colliders": scene.n_colliders, "joints": scene.n_joints,
             "springs": scene.n_springs, "steps": steps, "ms_per_step": ms / steps,
-            "body_steps_per_s": scene.n_bodies * steps / (ms / 1e3), "kernel_launches_per_step": launches}
+            "body_steps_per_s": scene.n_bodies * steps / (ms / 1e3), "kernel_launches_per_step": launches,
+            "cpu_baseline": cpu_general()}
 
 
 def literal_box_comparison(dev, steps=20, warmup=3, seed=2):
@@ -377,13 +462,53 @@ def literal_box_comparison(dev, steps=20, warmup=3, seed=2):
             "contacts_last_substep": contacts_last, "cell_scale": cell_scale}
 
 
-def adjoint_comparison(dev, steps=120, every=16, seed=5):
-    """256 worlds x 2,048 spheres with 1,024 springs each,
-    a 120-step forward pass (one CUDA-graph rollout) against the same
-    rollout recorded with a checkpoint every 16 steps plus the backward pass
-    (recompute each segment, then the adjoint substeps in reverse).  Timed
-    with CUDA events on the world's stream after one untimed round of each,
-    from the state those warm-up rounds leave."""
+def sparse_comparison(dev, seed=1):
+    """The 1,000-sphere walled world (600 steps at dt = 1/60) in full: the
+    GPU rollout (one step call per step, one CUDA-event pair around all 600)
+    against the oracle's single-threaded run of the same 600 steps, with the
+    two final states compared bit for bit."""
+    import numpy as np
+    import torch
+    from blobs_gb300 import native, scenes
+    from oracle import oracle
+    scene = scenes.sparse_spheres(seed=seed)
+    stream = torch.cuda.current_stream(dev)
+    w = native.World(scene, device=dev.index)
+    w.set_stream(stream.cuda_stream)
+    w.rollout(scene.dt, scene.n_steps)  # capture the graphs
+    w.load(scene)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(scene.n_steps):
+        w.step(scene.dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gpu_ms = e0.elapsed_time(e1)
+    got = w.read_bodies()
+    w.close()
+    o = oracle.OracleWorld(scene, 32, maintain_spatial_hash=True)
+    cpu_s = o.time_steps(scene.dt, scene.n_steps)
+    want = o.bodies()
+    exact = all(np.array_equal(got[k].astype(np.float64), want[k]) for k in ("pos", "pos_old", "vel"))
+    return {"bodies": scene.n_bodies, "steps": scene.n_steps, "gpu_ms": gpu_ms,
+            "gpu_ms_per_step": gpu_ms / scene.n_steps,
+            "gpu_sphere_steps_per_s": scene.n_bodies * scene.n_steps / (gpu_ms / 1e3),
+            "cpu_baseline": {"value": scene.n_bodies * scene.n_steps / cpu_s, "unit": "sphere-steps/s", "cores": 1,
+                             "kind": "port", "seconds": cpu_s,
+                             "sample": "the full 600-step run of the oracle, single-threaded"},
+            "speedup": cpu_s * 1e3 / gpu_ms, "final_state_bit_exact": exact}
+
+
+def adjoint_comparison(dev, steps=120, every=16, seed=5, finite_steps=32):
+    """256 worlds x 2,048 spheres with 1,024 springs each: a 120-step forward
+    pass (one CUDA-graph rollout) against the same rollout recorded with a
+    checkpoint every 16 steps plus the backward pass (recompute each
+    segment, then the adjoint substeps in reverse).  Every timed leg starts
+    from the scene's initial state (the world is reloaded before it) and
+    covers steps 0-119; each leg runs once untimed first (graph capture).
+    The same legs are timed over the first `finite_steps` steps, a horizon
+    whose gradients stay finite in f32."""
     import numpy as np
     import torch
     from blobs_gb300 import native, scenes
@@ -402,35 +527,61 @@ def adjoint_comparison(dev, steps=120, every=16, seed=5):
         g[idx] = 2.0 * (pos[idx] - tgt) / M
         return g
 
-    w.rollout(dt, steps)  # capture
-    w.rollout_record(dt, steps, every)  # capture the segment graph
-    gv, gk = w.backward(dl_dx(), scene.n_springs)
-    torch.cuda.synchronize()
-    e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
-    e0.record(stream)
-    w.rollout(dt, steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fwd_ms = e0.elapsed_time(e1)
-    e0.record(stream)
-    w.rollout_record(dt, steps, every)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    g = dl_dx()
-    e2.record(stream)
-    gv, gk = w.backward(g, scene.n_springs)
-    e3.record(stream)
-    torch.cuda.synchronize()
-    rec_ms, bwd_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
-    finite = bool(np.all(np.isfinite(gv)) and np.all(np.isfinite(gk)))
+    def legs(n):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        out = {}
+        for timed in (False, True):
+            w.load(scene)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            w.rollout(dt, n)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            fwd = e0.elapsed_time(e1)
+            w.load(scene)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            w.rollout_record(dt, n, every)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rec = e0.elapsed_time(e1)
+            g = dl_dx()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            gv, gk = w.backward(g, scene.n_springs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            bwd = e0.elapsed_time(e1)
+            if timed:
+                out = {"steps": n, "fwd_ms": fwd, "fwd_record_ms": rec, "bwd_ms": bwd,
+                       "fwd_bwd_over_fwd": (rec + bwd) / fwd,
+                       "gradients_finite": bool(np.all(np.isfinite(gv)) and np.all(np.isfinite(gk))),
+                       "max_abs_dl_dv0": float(np.nanmax(np.abs(gv)))}
+        return out
+
+    full = legs(steps)
+    short = legs(finite_steps)
     w.close()
+    cpu = cpu_gradient_batch(scene)
     return {"worlds": scene.n_worlds, "bodies": scene.n_bodies, "springs": scene.n_springs, "steps": steps,
-            "checkpoint_every": every, "fwd_ms": fwd_ms, "fwd_record_ms": rec_ms, "bwd_ms": bwd_ms,
-            "fwd_bwd_over_fwd": (rec_ms + bwd_ms) / fwd_ms,
-            "gradients_finite": finite,
+            "checkpoint_every": every, "fwd_ms": full["fwd_ms"], "fwd_record_ms": full["fwd_record_ms"],
+            "bwd_ms": full["bwd_ms"], "fwd_bwd_over_fwd": full["fwd_bwd_over_fwd"],
+            "gradients_finite": full["gradients_finite"],
+            "window": "every leg from the scene's initial state (reloaded before it): steps 0-%d" % (steps - 1),
+            "finite_horizon": short, "cpu_baseline": cpu,
             "note": "the derivative of this contact dynamics grows by orders of magnitude every few steps "
                     "(max |dL/dv0| of one world: 4e-2 at step 10, 1e1 at 15, 1e12 at 40, 1e84 at 120, f64), so "
-                    "the 120-step gradients overflow f32; the timing is of the full computation"}
+                    "the 120-step gradients overflow f32; finite_horizon times the same legs over the first "
+                    "%d steps, where they are finite" % finite_steps}
+
+
+def timed_positions(n_steps, warmup, steps):
+    """The K timed steps: evenly spaced over steps W .. n_steps-1 of the
+    rollout from t = 0 (every other step runs too, untimed)."""
+    span = n_steps - warmup
+    if steps > span:
+        raise SystemExit("--steps %d exceeds the %d steps after the warm-up" % (steps, span))
+    return [warmup + (i * span) // steps for i in range(steps)]
 
 
 def run_ours(args):
@@ -450,6 +601,7 @@ def run_ours(args):
 
     scene = scenes.dense_spheres(seed=2 + rank, n=args.n)
     dt = scene.dt
+    n_steps = scene.n_steps
     world = native.World(scene, device=local_rank)
     stream = torch.cuda.Stream(dev)          # graphs cannot be captured on the legacy default stream
     torch.cuda.set_stream(stream)
@@ -458,72 +610,82 @@ def run_ours(args):
     # the world is reloaded with the scene's initial state
     cell_scale = world.autotune(scene, dt, trial_steps=3)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 126 MB L2
+    timed = timed_positions(n_steps, args.warmup, args.steps)
+    timed_set = set(timed)
+    readouts = (1, 200, 500, n_steps)
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    def restart():
-        # every leg runs the same window of the scene: steps W .. W+K-1
-        # (the scene's contact load changes along a rollout)
-        world.load(scene)
-        for _ in range(args.warmup):
-            world.step(dt)
-        barrier()
-
-    for _ in range(args.warmup):
-        world.step(dt)
+    # -- timed region: the whole rollout from t = 0, every step between its own
+    # CUDA-event pair, L2 flushed before each; the K steps at `timed` make `value`
+    world.load(scene)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
+    counts = {}
+    launches = 0
     barrier()
-
-    # -- timed region: device time of K steps, L2 flushed before each --------
     clocks = Clocks(local_rank)
     clocks.start()
-    k0 = world.kernel_launches()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier()
-    for i in range(args.steps):
+    for i in range(n_steps):
         flush.zero_()
+        k0 = world.kernel_launches()
         starts[i].record(stream)
         world.step(dt)
         ends[i].record(stream)
+        if i in timed_set:
+            launches += world.kernel_launches() - k0
+        if i + 1 in readouts:  # synchronising reads, outside the events
+            counts[i + 1] = (world.contact_count()[1], world.walk_count()[1])
     barrier()
     clk = clocks.stop()
-    launches = world.kernel_launches() - k0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = max_over_ranks(sum(step_ms), dist, dev)
+    ms = np.array([s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)])
+    total_ms = max_over_ranks(float(ms[timed].sum()), dist, dev)
     value = job_throughput(scene.n_bodies, args.steps, world_size, total_ms)
+    rollout_ms = max_over_ranks(float(ms.sum()), dist, dev)
+    contacts_last = counts[n_steps][0]
 
-    contacts_total, contacts_last = world.contact_count()
+    def replay(mode):
+        """The same rollout again with per-phase events (mode "all") or
+        events around the contact kernel alone ("contact"), summed over the
+        timed steps."""
+        world.set_timing(True, contact_only=(mode == "contact"))
+        world.load(scene)
+        world.phase_times()
+        acc = {p_: [0.0, 0] for p_ in native.World.PHASES}
+        for i in range(n_steps):
+            if i in timed_set:
+                flush.zero_()
+            world.step(dt)
+            pt = world.phase_times()  # synchronising; clears the step's marks
+            if i in timed_set:
+                for p_, (t_, n_) in pt.items():
+                    acc[p_][0] += t_
+                    acc[p_][1] += n_
+        world.set_timing(False)
+        return acc
 
-    # -- per-phase kernel time (events captured into the step graph) ---------
-    world.set_timing(True)
-    restart()  # the instrumented graph is captured during the warm-up
-    world.phase_times()
-    phase = {p: [0.0, 0] for p in native.World.PHASES}
-    for i in range(args.steps):
-        flush.zero_()
-        world.step(dt)
-        for p, (ms, n) in world.phase_times().items():
-            phase[p][0] += ms
-            phase[p][1] += n
-    world.set_timing(False)
-    dom = max(phase, key=lambda p: phase[p][0])
-    dom_ms = phase[dom][0] / max(1, phase[dom][1])
+    phase = replay("all")
+    contact = replay("contact")["contact"]
+    dom_ms = contact[0] / max(1, contact[1])
     peak, peak_kind = peak_hbm()
-    alg_bytes = BYTES_CONTACT_PER_BODY * scene.n_bodies if dom == "contact" else None
-    achieved = alg_bytes / (dom_ms / 1e3) / 1e9 if alg_bytes else None
+    alg_bytes = BYTES_CONTACT_PER_BODY * scene.n_bodies
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
 
-    # -- end to end through the C ABI with pinned host buffers ----------------
+    # -- end to end through the C ABI with pinned host buffers, same steps ----
     n = scene.n_bodies
     h_pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
     h_old = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
     h_vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
-    restart()
-    world.read_bodies_into(h_pos, h_old, h_vel)
+    world.load(scene)
     e2e_s = []
-    for i in range(args.steps):
+    for i in range(n_steps):
+        if i not in timed_set:
+            world.step(dt)
+            continue
+        world.read_bodies_into(h_pos, h_old, h_vel)  # the host copy of the current state (untimed)
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -541,18 +703,31 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded dense_spheres generator: uniform positions with overlaps, N(0,0.5) velocities)",
         "config": {"workload": "1M spheres, r~U[0.05,0.15], 40%% packing (side %.1f, walled), g=(0,-9.81), "
-                               "dt=1/120, 8 substeps/step" % (float(scene.world_box[0, 2] * 2)),
+                               "dt=1/120, 8 substeps/step, 1,000-step rollout" % (float(scene.world_box[0, 2] * 2)),
                    "bodies": scene.n_bodies, "substeps": scene.substeps, "parallelism": "replicas" if world_size > 1
                    else "single", "l2": "flushed (256 MiB write) before every timed step",
                    "contacts_last_substep": contacts_last, "cell_scale": cell_scale,
-                   "window": "steps %d-%d of the scene; the phase-timing and end-to-end legs reload the scene and "
-                             "run the same window" % (args.warmup, args.warmup + args.steps - 1)},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                   "window": "the %d-step rollout from t=0 is run in full; the %d timed steps are evenly spaced over "
+                             "steps %d-%d (%s); the phase-timing and end-to-end legs reload the scene and time the "
+                             "same steps" % (n_steps, args.steps, args.warmup, n_steps - 1,
+                                             ",".join(map(str, timed)))},
+        "rollout": {"steps": n_steps, "ms_per_step": rollout_ms / n_steps,
+                    "value": job_throughput(scene.n_bodies, n_steps, world_size, rollout_ms),
+                    "ms_per_step_first_100": float(ms[:100].mean()), "ms_per_step_last_100": float(ms[-100:].mean()),
+                    "max_step_ms": float(ms.max()),
+                    "contacts_per_substep_after": {str(k): v[0] for k, v in counts.items()},
+                    "walk_bodies_per_substep_after": {str(k): v[1] for k, v in counts.items()},
+                    "note": "every step of the configuration's 1,000-step rollout from t=0, each between its own "
+                            "CUDA-event pair, L2 flushed before each (outside the events); the counts are of the "
+                            "last substep after 1, 200, 500 and 1,000 steps"},
+        "roofline": {"bound": "hbm", "kernel": "k_step_single (contact + integration)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": dom_ms,
+                     "timing": "CUDA events around the contact kernel alone, captured into the step graph, over "
+                               "the timed steps",
                      "traffic": profile_traffic("k_step_single_1M.md"),
                      "step_alg_GBps": whole_achieved, "step_frac": whole_achieved / peak},
-        "phases_ms_per_step": {p: phase[p][0] / args.steps for p in phase},
+        "phases_ms_per_step": {p_: phase[p_][0] / args.steps for p_ in phase},
         "e2e": {"value": e2e_value, "unit": "sphere-steps/s", "h2d_bytes_per_step": 16 * n,
                 "d2h_bytes_per_step": 24 * n},
         "gpu_launches": launches,
@@ -560,8 +735,10 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(target_n=scene.n_bodies)
+    world.close()
+    if rank == 0 and not args.no_sparse:
+        line["sparse_1k"] = sparse_comparison(dev)
     if rank == 0 and not args.no_batched:
-        world.close()
         line["batched"] = batched_comparison(dev)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_comparison(dev)
@@ -569,7 +746,6 @@ def run_ours(args):
         line["general"] = general_comparison(dev)
     if rank == 0 and not args.no_literal:
         line["literal_box"] = literal_box_comparison(dev)
-    world.close()
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -589,6 +765,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-general", action="store_true")
     ap.add_argument("--no-literal", action="store_true", help="skip the 2000 x 2000 literal-box run")
+    ap.add_argument("--no-sparse", action="store_true", help="skip the 1,000-sphere full-run comparison")
     ap.add_argument("--section", choices=["general", "batched"], default=None,
                     help="run one secondary workload alone (profiling driver), print its phase times")
     args = ap.parse_args()

@@ -23,7 +23,7 @@ enum : uint8_t {
 // Device status bits, read back by the host after a synchronising call.
 enum : uint32_t {
   ST_NAN = 1u,         // NaN contact normal or non-finite rotation (physics.rs:293, 471-474)
-  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (reserved: no kernel waits on another)
+  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (the single-pass scan's look-back)
   ST_BAD_INDEX = 4u,   // a device bounds check fired
 };
 
@@ -121,6 +121,10 @@ struct WorldDev {
   uint8_t* ccount;           // general path, per collider: contacts in clist
   uint8_t* bslow;            // general path, per body: contacts need the ordered walk (zero between substeps)
   uint32_t* tile_sums;       // per scan tile
+  // single-pass scan (NULL: the two-kernel scan): [0] the tile ticket,
+  // [1 + t] tile t's published value: (epoch * 4 + state) << 32 | sum, state
+  // 1 = the tile's own sum, 2 = the sum of every tile up to and including it
+  unsigned long long* scan_state;
 
   // single-sphere path: body storage re-sorted into cell order once per step
   float4* sa[2];             // (snapshot x, y, radius, arena id bits), double-buffered per substep
@@ -131,6 +135,8 @@ struct WorldDev {
   uint32_t* key;             // per storage slot: cell of the snapshot for the next substep
   uint32_t* ckey;            // per storage slot: cell the permute sorted the body into
   uint32_t* where;           // arena id -> storage slot
+  uint32_t* defer_list;      // storage slots whose substep k_step_deferred finishes (plain steps)
+  uint32_t* defer_count;     // entries of defer_list this substep (zeroed by the cell scan)
 
   // collision event stream (NULL when off): one record per resolved pair,
   // appended in any order and put in the reference's order on the host by
@@ -145,6 +151,8 @@ struct WorldDev {
   unsigned long long* contacts_total;
   unsigned long long* pushouts_total;
   uint32_t* contacts_sub;    // contacts of the most recent substep
+  unsigned long long* walk_total;  // bodies whose contacts took the exact selection walk (many candidates)
+  uint32_t* walk_sub;        // the same in the most recent substep
   uint32_t* status;
 };
 
@@ -296,6 +304,7 @@ __device__ __forceinline__ void record_event(const WorldDev& w, uint32_t a, uint
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // polls of a predecessor tile before ST_TIMEOUT
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
 constexpr uint32_t CL_CAP = 8;             // general path: contacts kept per collider
 constexpr uint32_t COUNTER_BINS = 64;

@@ -28,6 +28,8 @@ void launch_emit_pairs(const WorldDev& w, bool multiworld, uint32_t mode, uint32
 void launch_permute(const WorldDev& w, const SingleArgs& a, cudaStream_t st);
 void launch_scatter_cand(const WorldDev& w, const float4* a_in, float4* cand, cudaStream_t st);
 void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st);
+// the bodies the plain step deferred (after launch_step_single, same args)
+void launch_step_deferred(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st);
 void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st);
 void launch_gather_single(const WorldDev& w, const float4* A, const float4* B, const float2* V, float2* pos,
                           float2* pos_old, float2* vel, float2* snap, float v_div, cudaStream_t st);

@@ -163,13 +163,14 @@ __device__ __forceinline__ void single_event(const WorldDev& w, const SingleArgs
   record_event(w, c, lo, a.v_in[j], a.v_in[jl]);
 }
 
-__device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush) {
+__device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush, bool walked) {
   uint32_t t = ncontacts, p = npush;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     t += __shfl_xor_sync(0xffffffffu, t, o);
     p += __shfl_xor_sync(0xffffffffu, p, o);
   }
+  const uint32_t nw = __popc(__ballot_sync(0xffffffffu, walked));
   if ((threadIdx.x & 31u) == 0u) {
     const uint32_t bin = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (COUNTER_BINS - 1);
     if (t) {
@@ -177,6 +178,10 @@ __device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts
       atomicAdd(w.contacts_sub + bin, t);
     }
     if (p) atomicAdd(w.pushouts_total + bin, (unsigned long long)p);
+    if (nw) {
+      atomicAdd(w.walk_total + bin, (unsigned long long)nw);
+      atomicAdd(w.walk_sub + bin, nw);
+    }
   }
 }
 
@@ -256,7 +261,167 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
   return p;
 }
 
+// The warp's candidate tests, spread over its lanes.  Every lane (body) has
+// its 3 row ranges of candidates; the warp lists all (body, candidate) pairs
+// body by body (rows in order, candidates ascending), and in each round its
+// 32 lanes test 32 consecutive pairs of that list, so every lane does the
+// same work however unevenly the candidates fall on the bodies.  The near
+// bits come back as one 32-bit word per round; each body then reads its own
+// bits.  Per warp in shared memory: the bodies' records and their row
+// offsets into the pair list, the owner (lane) of every pair, the words.
+constexpr uint32_t COOP_PAIRS = 1024;  // pairs per warp; a warp with more takes the per-lane pass
+constexpr int STEP_THREADS = 256;
+
+struct CoopWarp {
+  float4 body[32];                     // snapshot x, y, radius, arena id bits
+  int4 geo[32];                        // position - pair index for rows 0, 1, 2; first pair of row 1
+  int row2[32];                        // first pair of row 2
+  uint32_t words[COOP_PAIRS / 32 + 2]; // near bits of the pair list
+  uint8_t owner[COOP_PAIRS];           // lane of each pair
+};
+
+// Bodies with more near candidates than this take k_step_deferred.
+constexpr uint32_t DEFER_NEAR = 12;
+constexpr uint32_t DEFER_CAP = 256;    // contacts a deferred body's warp ranks in shared memory
+constexpr int DEFER_THREADS = 128;
+constexpr uint32_t DEFER_BLOCKS = 152 * 8;
+
+struct DeferWarp {
+  uint32_t id[DEFER_CAP];              // partner arena id of each contact found
+  float4 corr[DEFER_CAP];              // correction x, y; push-out flag bits
+  uint32_t order[DEFER_CAP];           // contacts in ascending partner id
+};
+
+// Phase 2: the near candidates of body c in ascending arena id (the
+// reference's pair order for this body, physics.rs:244-249), the warp's
+// lanes in step.  Bit t of `near` is candidate t of the rows starting at
+// cell-order positions s0, s1, s2 and at bits 0, t1, t2.
+template <int MODE, bool HOOKS>
+__device__ __forceinline__ float2 apply_near(const WorldDev& w, const SingleArgs& a, unsigned long long near,
+                                             uint32_t s0, uint32_t s1, uint32_t s2, uint32_t t1, uint32_t t2,
+                                             uint32_t j, uint32_t c, float2 p0, float2 s, float r, float m,
+                                             uint32_t& ncontacts, uint32_t& npush, uint32_t& nrec) {
+  const float4* __restrict__ C = a.cand;
+  float2 p = p0;
+  while (near) {
+    unsigned long long best_bit = 0ull;
+    uint32_t best = 0xffffffffu;
+    float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
+      const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
+      const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
+      const float4 o = C[q];
+      const uint32_t c2 = __float_as_uint(o.w);
+      if (c2 < best) {
+        best = c2;
+        bo = o;
+        best_bit = mk & (~mk + 1ull);
+      }
+      if ((near & (near - 1ull)) == 0ull) break;  // one near candidate needs no ordering
+    }
+    near &= ~best_bit;
+    if (best >= w.n_bodies || best == c) continue;
+    const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
+    SinglePair sp;
+    if (!single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
+    if (sp.pushed) p = add(p, sp.push);
+    p = add(p, sp.corr);
+    if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
+    if (best < c) {
+      ++ncontacts;
+      npush += sp.pushed ? 1u : 0u;
+      if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
+    }
+  }
+  return p;
+}
+
 }  // namespace
+
+// update_objects (physics.rs:323-367) of one body after its contacts:
+// gravity + springs at the start-of-substep state, Verlet, the snapshot, the
+// constraints, and the next substep's cell key and rank.  p0 is the position
+// at the start of the substep, p the position after the contacts.
+template <int MODE>
+__device__ __forceinline__ void finish_single(const WorldDev& w, const SingleArgs& a, const WorldParam& wp,
+                                              const BodyConst& k, uint32_t j, uint32_t c, float4 av, float4 bv,
+                                              float2 p0, float2 p) {
+  const float r = av.z;
+  // ---- update_objects (physics.rs:323-367) with gravity + springs ----
+  const float dt = a.dt;
+  float2 po, vel;
+  if (k.flags & BF_STATIC) {
+    po = p;
+    vel = v2(0.0f, 0.0f);
+  } else {
+    po = v2(bv.z, bv.w);
+    uint32_t fl = k.flags;
+    if (a.pending && MODE == 0) fl |= rec_flags(w.body_c[c]);
+    if (a.pending && (fl & BF_VREQ)) po = sub(p, mul(w.vreq[c], dt));
+    const float ratio = (fl & BF_FIRST_DYN) ? a.ratio_first : a.ratio_rest;
+    const float2 disp = mul(sub(p, po), ratio);
+    float2 acc = a.pending ? w.pend_acc[c] : v2(0.0f, 0.0f);
+    acc = add(acc, mul(w.gravity, k.gm));
+    if (a.springs) {
+      const uint32_t q0 = w.body_spr_start[c], q1 = w.body_spr_start[c + 1];
+      for (uint32_t qq = q0; qq < q1; ++qq) {
+        const uint32_t e = w.body_spr[qq];
+        const uint32_t sidx = e >> 1;
+        const uint32_t other = (e & 1u) ? w.spr_a[sidx] : w.spr_b[sidx];
+        const uint32_t so = w.where[other];
+        const float4 bo = a.b_in[so];
+        const float2 po_pos = v2(bo.x, bo.y);
+        const float2 po_vel = a.v_in[so];
+        const float2 own_vel = a.v_in[j];
+        const float2 va = (e & 1u) ? po_vel : own_vel, vb = (e & 1u) ? own_vel : po_vel;
+        const float2 pa = (e & 1u) ? po_pos : p0, pb = (e & 1u) ? p0 : po_pos;
+        const float2 d = sub(pb, pa);
+        const float dist = len2(d);
+        const float2 dir = divs(d, dist);
+        const float2 rv = sub(va, vb);
+        const float2 damping = mul(dir, w.spr_c[sidx] * dot2(rv, dir));
+        const float sk = w.spr_k[sidx] * (dist - w.spr_rest[sidx]);
+        const float2 fm = v2(sk - damping.x, sk - damping.y);  // springs.rs:41 broadcast
+        float2 f = mulv(dir, fm);
+        if (e & 1u) f = v2(-f.x, -f.y);
+        acc = add(acc, divs(f, k.m));
+      }
+    }
+    po = p;
+    p = add(p, add(disp, mul(mul(acc, dt), dt)));
+    if (a.rot_dynamic) {
+      const float tq = a.pending ? w.pend_torque[c] : 0.0f;
+      float avl = w.angvel[c];
+      avl = avl + (tq / w.inertia[c]) * dt;
+      w.angvel[c] = avl;
+      w.rot[c] = w.rot[c] + avl * dt;
+    }
+    // calculated_velocity = disp / dt (physics.rs:357); without springs or
+    // collision events nothing reads it during the step, so the
+    // displacement is kept and divided when it is read
+    vel = a.v_vel ? divs(disp, dt) : disp;
+  }
+  const float2 snap = v2(0.0f + p.x, 0.0f + p.y);  // rot(theta) * 0 + p
+  for (uint32_t kk = 0; kk < w.n_circles; ++kk) {
+    const float2 cc = v2(w.circles[3 * kk], w.circles[3 * kk + 1]);
+    const float radius = w.circles[3 * kk + 2];
+    const float2 to = sub(p, cc);
+    const float dist = len2(to);
+    if (dist > radius) p = add(cc, mul(divs(to, dist), radius));
+  }
+  if (wp.has_box) {
+    p.x = fminf(fmaxf(p.x, wp.box_lo_x + k.br), wp.box_hi_x - k.br);
+    p.y = fminf(fmaxf(p.y, wp.box_lo_y + k.br), wp.box_hi_y - k.br);
+  }
+  a.a_out[j] = make_float4(snap.x, snap.y, r, av.w);
+  a.b_out[j] = make_float4(p.x, p.y, po.x, po.y);
+  if (a.v_vel || a.write_v) a.v_out[j] = vel;
+  if (a.do_keys) {
+    const uint32_t key = cell_key(wp, snap);
+    w.key[j] = key;
+    w.rank[j] = atomicAdd(w.cell_count + key, 1u);
+  }
+}
 
 // Storage slot i -> its position in this substep's cell order.
 __global__ void __launch_bounds__(256) k_permute(WorldDev w, SingleArgs a) {
@@ -291,89 +456,140 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 }
 
 // HOOKS: compiled with the adjoint's contact recording and the collision
-// event stream (the plain step leaves their branches out).
+// event stream (the plain step leaves their branches out, and spreads its
+// candidate tests over the warp's lanes).
 template <int MODE, bool HOOKS>
-__global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a) {
+__global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, SingleArgs a) {
+  constexpr bool COOP = !HOOKS;
+  __shared__ CoopWarp coop_smem[COOP ? STEP_THREADS / 32 : 1];
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool active = j < w.n_bodies;
   uint32_t ncontacts = 0, npush = 0;
-  if (j < w.n_bodies) {
-    const float4 av = a.a_in[j];
-    const float4 bv = a.b_in[j];
-    uint32_t c = __float_as_uint(av.w);
+  bool walked = false;
+  bool deferred = false;  // contacts (and the rest of the body's substep) left to k_step_deferred
+
+  float4 av = make_float4(0.f, 0.f, 0.f, 0.f), bv = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t c = 0;
+  if (active) {
+    av = a.a_in[j];
+    bv = a.b_in[j];
+    c = __float_as_uint(av.w);
     if (c >= w.n_bodies) {
       atomicOr(w.status, ST_BAD_INDEX);
       c = 0;
     }
-    const float2 s = v2(av.x, av.y);
-    const float r = av.z;
-    const WorldParam wp0 = w.wparam[0];
-    const BodyConst k = body_const<MODE>(w, wp0, c, r);
-    const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
+  }
+  const float2 s = v2(av.x, av.y);
+  const float r = av.z;
+  const WorldParam wp0 = w.wparam[0];
+  const BodyConst k = body_const<MODE>(w, wp0, c, r);
+  const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
+
+  // the 3 candidate rows of a body away from the grid edge: contiguous
+  // ranges of the cell-order array
+  const uint32_t own_key = (active && a.contacts) ? a.own_cell[j] : 0u;
+  const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
+  const uint32_t lx = (own_key - wp.cell_base) & wm, ly = (own_key - wp.cell_base) >> wp.log2w;
+  const bool interior = active && a.contacts && lx >= 1u && lx < wm && ly >= 1u && ly < hm;
+  uint32_t s0 = 0, s1 = 0, s2 = 0, l0 = 0, l1 = 0, l2 = 0;
+  if (interior) {
+    const uint32_t n = w.n_bodies;
+    const uint32_t r1 = own_key - 1u, r0 = r1 - (wm + 1u), r2 = r1 + (wm + 1u);
+    s0 = w.cell_start[r0];
+    s1 = w.cell_start[r1];
+    s2 = w.cell_start[r2];
+    const uint32_t e0 = min(w.cell_start[r0 + 3u], n), e1 = min(w.cell_start[r1 + 3u], n),
+                   e2 = min(w.cell_start[r2 + 3u], n);
+    l0 = e0 > s0 ? e0 - s0 : 0u;
+    l1 = e1 > s1 ? e1 - s1 : 0u;
+    l2 = e2 > s2 ? e2 - s2 : 0u;
+  }
+
+  // Phase 1, spread over the warp (plain steps): near bits of every body
+  // whose rows hold at most 64 candidates.
+  unsigned long long near = 0ull;
+  bool coop_done = false;
+  if (COOP && a.contacts) {
+    const uint32_t tot = l0 + l1 + l2;
+    const uint32_t nl = (interior && tot <= 64u) ? tot : 0u;
+    uint32_t incl = nl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t off = incl - nl;
+    if (total <= COOP_PAIRS) {  // warp-uniform
+      CoopWarp& S = coop_smem[COOP ? (threadIdx.x >> 5) : 0];
+      S.body[lane] = make_float4(s.x, s.y, r, av.w);
+      S.geo[lane] = make_int4((int)s0 - (int)off, (int)s1 - (int)(off + l0), (int)s2 - (int)(off + l0 + l1),
+                              (int)(off + l0));
+      S.row2[lane] = (int)(off + l0 + l1);
+      for (uint32_t t = 0; t < nl; ++t) S.owner[off + t] = (uint8_t)lane;
+      __syncwarp();
+      const float4* __restrict__ C = a.cand;
+      for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t q = base + lane;
+        bool nr = false;
+        if (q < total) {
+          const uint32_t ow = S.owner[q];
+          const float4 ob = S.body[ow];
+          const int4 g = S.geo[ow];
+          const int pq = (int)q;
+          const int d = pq < g.w ? g.x : (pq < S.row2[ow] ? g.y : g.z);
+          const float4 o = C[pq + d];
+          nr = near_pair(ob.x - o.x, ob.y - o.y, ob.z + o.z) && __float_as_uint(o.w) != __float_as_uint(ob.w);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, nr);
+        if (lane == 0) S.words[base >> 5] = bal;
+      }
+      __syncwarp();
+      if (nl) {
+        const uint32_t w0 = off >> 5, sh = off & 31u;
+        const unsigned long long lo = (unsigned long long)S.words[w0] | ((unsigned long long)S.words[w0 + 1] << 32);
+        near = lo >> sh;
+        if (sh) near |= (unsigned long long)S.words[w0 + 2] << (64u - sh);
+        if (nl < 64u) near &= (1ull << nl) - 1ull;
+        coop_done = true;
+      }
+      __syncwarp();  // the warp's next use of S (none in this launch) comes after every read
+    }
+  }
+
+  if (active) {
     const float2 p0 = v2(bv.x, bv.y);  // position at the start of the substep
     float2 p = p0;
     uint32_t nrec = 0;  // contacts recorded for the adjoint
 
-    const uint32_t own_key = a.contacts ? a.own_cell[j] : 0u;
-    const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
-    const uint32_t lx = (own_key - wp.cell_base) & wm, ly = (own_key - wp.cell_base) >> wp.log2w;
-    const bool interior = lx >= 1u && lx < wm && ly >= 1u && ly < hm;
-    if (a.contacts && interior) {
-      // Cells away from the grid edge: the 3x3 block is three contiguous
-      // ranges of the cell-order array, one per row.
-      const float4* __restrict__ C = a.cand;
-      const uint32_t n = w.n_bodies;
-      const uint32_t r1 = own_key - 1u, r0 = r1 - (wm + 1u), r2 = r1 + (wm + 1u);
-      const uint32_t s0 = w.cell_start[r0], s1 = w.cell_start[r1], s2 = w.cell_start[r2];
-      const uint32_t e0 = min(w.cell_start[r0 + 3u], n), e1 = min(w.cell_start[r1 + 3u], n),
-                     e2 = min(w.cell_start[r2 + 3u], n);
-      const uint32_t l0 = e0 > s0 ? e0 - s0 : 0u, l1 = e1 > s1 ? e1 - s1 : 0u, l2 = e2 > s2 ? e2 - s2 : 0u;
+    if (COOP && coop_done) {
+      // Phase 2 on the warp's near bits (rows at bits 0, l0, l0 + l1); a
+      // body with many near candidates is left to a warp of its own
+      if (__popcll(near) > DEFER_NEAR) deferred = true;
+      else
+        p = apply_near<MODE, HOOKS>(w, a, near, s0, s1, s2, l0, l0 + l1, j, c, p0, s, r, k.m, ncontacts, npush,
+                                    nrec);
+    } else if (interior) {
       // bit positions are padded to multiples of 4 per row: they must fit 64
       if (((l0 + 3u) & ~3u) + ((l1 + 3u) & ~3u) + ((l2 + 3u) & ~3u) <= 64u) {
-        // Phase 1: squared-distance test per candidate (self included, it is
-        // skipped below); near candidates become bits of their position
-        // (row 0 at bit 0, row 1 at bit 4*ceil(l0/4), ...).
-        unsigned long long near = 0ull;
+        // Phase 1 per lane: squared-distance test per candidate (self
+        // excluded); near candidates become bits of their position (row 0
+        // at bit 0, row 1 at bit 4*ceil(l0/4), ...).
+        const float4* __restrict__ C = a.cand;
+        unsigned long long nb = 0ull;
         uint32_t t = 0;
-        near_range(C, s, r, c, s0, s0 + l0, t, near);
+        near_range(C, s, r, c, s0, s0 + l0, t, nb);
         const uint32_t t1 = t;
-        near_range(C, s, r, c, s1, s1 + l1, t, near);
+        near_range(C, s, r, c, s1, s1 + l1, t, nb);
         const uint32_t t2 = t;
-        near_range(C, s, r, c, s2, s2 + l2, t, near);
-        // Phase 2: the near candidates in ascending arena id (the
-        // reference's pair order for this body), the warp's lanes in step.
-        // One near candidate needs no ordering.
-        while (near) {
-          unsigned long long best_bit = 0ull;
-          uint32_t best = 0xffffffffu;
-          float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
-            const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
-            const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
-            const float4 o = C[q];
-            const uint32_t c2 = __float_as_uint(o.w);
-            if (c2 < best) {
-              best = c2;
-              bo = o;
-              best_bit = mk & (~mk + 1ull);
-            }
-            if ((near & (near - 1ull)) == 0ull) break;
-          }
-          near &= ~best_bit;
-          if (best >= w.n_bodies || best == c) continue;
-          const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
-          SinglePair sp;
-          if (!single_pair(w, a, c, p0, s, r, k.m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
-          if (sp.pushed) p = add(p, sp.push);
-          p = add(p, sp.corr);
-          if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
-          if (best < c) {
-            ++ncontacts;
-            npush += sp.pushed ? 1u : 0u;
-            if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
-          }
-        }
+        near_range(C, s, r, c, s2, s2 + l2, t, nb);
+        p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+      } else if (COOP) {
+        deferred = true;
       } else {
         p = contacts_walk<MODE, HOOKS>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+        walked = true;
       }
     } else if (a.contacts) {
       // cells on the grid edge (the torus wraps): general segments
@@ -384,23 +600,23 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
         // Phase 1: one squared-distance test per candidate (self included:
         // it is skipped below); near candidates become bits of their
         // position in the 3x3 enumeration.
-        unsigned long long near = 0ull;
+        unsigned long long nb = 0ull;
         uint32_t t = 0;
 #pragma unroll
         for (int sg = 0; sg < 6; ++sg) {
           const uint32_t q1 = g.s[sg] + g.l[sg];
           for (uint32_t q = g.s[sg]; q < q1; ++q, ++t) {
             const float4 o = C[q];
-            if (near_pair(s.x - o.x, s.y - o.y, r + o.z)) near |= 1ull << t;
+            if (near_pair(s.x - o.x, s.y - o.y, r + o.z)) nb |= 1ull << t;
           }
         }
         // Phase 2: the near candidates in ascending arena id (the
         // reference's pair order for this body), the warp's lanes in step.
-        while (near) {
+        while (nb) {
           unsigned long long best_bit = 0ull;
           uint32_t best = 0xffffffffu;
           float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
+          for (unsigned long long mk = nb; mk; mk &= mk - 1ull) {
             const float4 o = C[slot_of(g, (uint32_t)(__ffsll((long long)mk) - 1))];
             const uint32_t c2 = __float_as_uint(o.w);
             if (c2 < best) {
@@ -409,7 +625,7 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
               best_bit = mk & (~mk + 1ull);
             }
           }
-          near &= ~best_bit;
+          nb &= ~best_bit;
           if (best >= w.n_bodies || best == c) continue;
           const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
           SinglePair sp;
@@ -423,8 +639,11 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
             if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
           }
         }
+      } else if (COOP) {
+        deferred = true;
       } else {
         p = contacts_walk<MODE, HOOKS>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+        walked = true;
       }
     }
 
@@ -433,82 +652,131 @@ __global__ void __launch_bounds__(256, 4) k_step_single(WorldDev w, SingleArgs a
       if (nrec) atomicMax(a.rec_max, nrec);
     }
 
-    // ---- update_objects (physics.rs:323-367) with gravity + springs ----
-    const float dt = a.dt;
-    float2 po, vel;
-    if (k.flags & BF_STATIC) {
-      po = p;
-      vel = v2(0.0f, 0.0f);
-    } else {
-      po = v2(bv.z, bv.w);
-      uint32_t fl = k.flags;
-      if (a.pending && MODE == 0) fl |= rec_flags(w.body_c[c]);
-      if (a.pending && (fl & BF_VREQ)) po = sub(p, mul(w.vreq[c], dt));
-      const float ratio = (fl & BF_FIRST_DYN) ? a.ratio_first : a.ratio_rest;
-      const float2 disp = mul(sub(p, po), ratio);
-      float2 acc = a.pending ? w.pend_acc[c] : v2(0.0f, 0.0f);
-      acc = add(acc, mul(w.gravity, k.gm));
-      if (a.springs) {
-        const uint32_t q0 = w.body_spr_start[c], q1 = w.body_spr_start[c + 1];
-        for (uint32_t qq = q0; qq < q1; ++qq) {
-          const uint32_t e = w.body_spr[qq];
-          const uint32_t sidx = e >> 1;
-          const uint32_t other = (e & 1u) ? w.spr_a[sidx] : w.spr_b[sidx];
-          const uint32_t so = w.where[other];
-          const float4 bo = a.b_in[so];
-          const float2 po_pos = v2(bo.x, bo.y);
-          const float2 po_vel = a.v_in[so];
-          const float2 own_vel = a.v_in[j];
-          const float2 va = (e & 1u) ? po_vel : own_vel, vb = (e & 1u) ? own_vel : po_vel;
-          const float2 pa = (e & 1u) ? po_pos : p0, pb = (e & 1u) ? p0 : po_pos;
-          const float2 d = sub(pb, pa);
-          const float dist = len2(d);
-          const float2 dir = divs(d, dist);
-          const float2 rv = sub(va, vb);
-          const float2 damping = mul(dir, w.spr_c[sidx] * dot2(rv, dir));
-          const float sk = w.spr_k[sidx] * (dist - w.spr_rest[sidx]);
-          const float2 fm = v2(sk - damping.x, sk - damping.y);  // springs.rs:41 broadcast
-          float2 f = mulv(dir, fm);
-          if (e & 1u) f = v2(-f.x, -f.y);
-          acc = add(acc, divs(f, k.m));
-        }
+    if (!deferred) finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
+  }
+  if (COOP && a.contacts) {
+    // append the deferred bodies to the list k_step_deferred works through
+    const uint32_t dm = __ballot_sync(0xffffffffu, deferred);
+    if (dm) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(w.defer_count, (uint32_t)__popc(dm));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const uint32_t at = base + (uint32_t)__popc(dm & ((1u << lane) - 1u));
+      if (deferred) {
+        if (at < w.n_bodies) w.defer_list[at] = j;
+        else atomicOr(w.status, ST_BAD_INDEX);
       }
-      po = p;
-      p = add(p, add(disp, mul(mul(acc, dt), dt)));
-      if (a.rot_dynamic) {
-        const float tq = a.pending ? w.pend_torque[c] : 0.0f;
-        float avl = w.angvel[c];
-        avl = avl + (tq / w.inertia[c]) * dt;
-        w.angvel[c] = avl;
-        w.rot[c] = w.rot[c] + avl * dt;
-      }
-      // calculated_velocity = disp / dt (physics.rs:357); without springs or
-      // collision events nothing reads it during the step, so the
-      // displacement is kept and divided when it is read
-      vel = a.v_vel ? divs(disp, dt) : disp;
-    }
-    const float2 snap = v2(0.0f + p.x, 0.0f + p.y);  // rot(theta) * 0 + p
-    for (uint32_t kk = 0; kk < w.n_circles; ++kk) {
-      const float2 cc = v2(w.circles[3 * kk], w.circles[3 * kk + 1]);
-      const float radius = w.circles[3 * kk + 2];
-      const float2 to = sub(p, cc);
-      const float dist = len2(to);
-      if (dist > radius) p = add(cc, mul(divs(to, dist), radius));
-    }
-    if (wp.has_box) {
-      p.x = fminf(fmaxf(p.x, wp.box_lo_x + k.br), wp.box_hi_x - k.br);
-      p.y = fminf(fmaxf(p.y, wp.box_lo_y + k.br), wp.box_hi_y - k.br);
-    }
-    a.a_out[j] = make_float4(snap.x, snap.y, r, av.w);
-    a.b_out[j] = make_float4(p.x, p.y, po.x, po.y);
-    if (a.v_vel || a.write_v) a.v_out[j] = vel;
-    if (a.do_keys) {
-      const uint32_t key = cell_key(wp, snap);
-      w.key[j] = key;
-      w.rank[j] = atomicAdd(w.cell_count + key, 1u);
     }
   }
-  if (a.contacts) count_warp(w, ncontacts, npush);
+  if (a.contacts) count_warp(w, ncontacts, npush, walked || deferred);
+}
+
+// The bodies k_step_single deferred (many candidates or many near
+// candidates), one warp each: the warp's lanes test the 3x3 candidates
+// together with the reference's exact test and compute each contact's
+// correction (each depends only on the snapshots, masses and start-of-substep
+// positions), the contacts are ranked by partner id in shared memory, and
+// one lane applies them in that order -- the reference's pair order for this
+// body -- then finishes the body's substep.  More than DEFER_CAP contacts:
+// the exact selection walk on one lane.
+template <int MODE>
+__global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, SingleArgs a) {
+  __shared__ DeferWarp dsm[DEFER_THREADS / 32];
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  DeferWarp& S = dsm[wib];
+  const uint32_t n = w.n_bodies;
+  const uint32_t n_def = min(*w.defer_count, n);
+  const uint32_t gw = blockIdx.x * (DEFER_THREADS / 32) + wib, nwarps = gridDim.x * (DEFER_THREADS / 32);
+  const WorldParam wp0 = w.wparam[0];
+  uint32_t tc = 0, tp = 0;
+  for (uint32_t it = gw; it < n_def; it += nwarps) {
+    const uint32_t j = w.defer_list[it];
+    if (j >= n) {
+      if (lane == 0) atomicOr(w.status, ST_BAD_INDEX);
+      continue;
+    }
+    const float4 av = a.a_in[j], bv = a.b_in[j];
+    uint32_t c = __float_as_uint(av.w);
+    if (c >= n) {
+      if (lane == 0) atomicOr(w.status, ST_BAD_INDEX);
+      c = 0;
+    }
+    const float2 s = v2(av.x, av.y);
+    const float r = av.z;
+    const BodyConst k = body_const<MODE>(w, wp0, c, r);
+    const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
+    const float2 p0 = v2(bv.x, bv.y);
+    const Segments g = segments(w, wp, a.own_cell[j]);
+    const uint32_t m = g.l[0] + g.l[1] + g.l[2] + g.l[3] + g.l[4] + g.l[5];
+    uint32_t cnt = 0;
+    for (uint32_t t0 = 0; t0 < m; t0 += 32u) {
+      const uint32_t t = t0 + lane;
+      bool hit = false;
+      SinglePair sp;
+      uint32_t c2 = 0;
+      if (t < m) {
+        const float4 o = a.cand[slot_of(g, t)];
+        c2 = __float_as_uint(o.w);
+        if (c2 != c && c2 < n) {
+          const float m2 = (MODE == 0 || a.mass4r) ? o.z * 4.0f : w.body_c[c2].x;
+          hit = single_pair(w, a, c, p0, s, r, k.m, c2, v2(o.x, o.y), o.z, m2, sp);
+        }
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, hit);
+      const uint32_t at = cnt + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+      if (hit && at < DEFER_CAP) {
+        S.id[at] = c2;
+        S.corr[at] = make_float4(sp.corr.x, sp.corr.y, __uint_as_float(sp.pushed ? 1u : 0u), 0.0f);
+      }
+      cnt += (uint32_t)__popc(bal);
+    }
+    __syncwarp();
+    if (cnt <= DEFER_CAP) {
+      // rank of every contact by partner id (ids are distinct)
+      for (uint32_t e = lane; e < cnt; e += 32u) {
+        const uint32_t ide = S.id[e];
+        uint32_t rank = 0;
+        for (uint32_t f = 0; f < cnt; ++f) rank += S.id[f] < ide ? 1u : 0u;
+        S.order[rank] = e;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        float2 p = p0;
+        for (uint32_t i = 0; i < cnt; ++i) {
+          const uint32_t e = S.order[i];
+          if (e >= cnt) {  // ranks are a permutation when the partner ids are distinct
+            atomicOr(w.status, ST_BAD_INDEX);
+            continue;
+          }
+          const uint32_t c2 = S.id[e];
+          const float4 cr = S.corr[e];
+          const bool pushed = __float_as_uint(cr.z) != 0u;
+          if (pushed) p = add(p, c > c2 ? v2(0.01f, 0.0f) : v2(-0.01f, -0.0f));
+          p = add(p, v2(cr.x, cr.y));
+          if (c2 < c) {
+            ++tc;
+            tp += pushed ? 1u : 0u;
+          }
+        }
+        finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
+      }
+    } else if (lane == 0) {
+      uint32_t nc = 0, np = 0, nr = 0;
+      const float2 p = contacts_walk<MODE, false>(w, a, g, j, c, p0, s, r, k.m, nc, np, nr);
+      tc += nc;
+      tp += np;
+      finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && (tc || tp)) {
+    const uint32_t bin = gw & (COUNTER_BINS - 1);
+    if (tc) {
+      atomicAdd(w.contacts_total + bin, (unsigned long long)tc);
+      atomicAdd(w.contacts_sub + bin, tc);
+    }
+    if (tp) atomicAdd(w.pushouts_total + bin, (unsigned long long)tp);
+  }
 }
 
 // Keys and ranks of the current storage (after a load or a host write).
@@ -603,6 +871,13 @@ void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaSt
     else if (mode == 1) k_step_single<1, false><<<g, 256, 0, st>>>(w, a);
     else k_step_single<2, false><<<g, 256, 0, st>>>(w, a);
   }
+}
+
+void launch_step_deferred(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st) {
+  if (!w.n_bodies || !w.defer_list) return;
+  if (mode == 0) k_step_deferred<0><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+  else if (mode == 1) k_step_deferred<1><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+  else k_step_deferred<2><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
 }
 
 void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st) {

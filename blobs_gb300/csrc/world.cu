@@ -26,11 +26,23 @@ struct Counters {
   unsigned long long contacts_total[COUNTER_BINS];
   unsigned long long pushouts_total[COUNTER_BINS];
   uint32_t contacts_sub[COUNTER_BINS];
+  unsigned long long walk_total[COUNTER_BINS];
+  uint32_t walk_sub[COUNTER_BINS];
   uint32_t status;
   uint32_t pad[3];
   unsigned long long contacts() const {
     unsigned long long t = 0;
     for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += contacts_total[i];
+    return t;
+  }
+  unsigned long long walks() const {
+    unsigned long long t = 0;
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += walk_total[i];
+    return t;
+  }
+  unsigned long long walks_sub() const {
+    unsigned long long t = 0;
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += walk_sub[i];
     return t;
   }
   unsigned long long pushouts() const {
@@ -150,7 +162,8 @@ struct blobs_world {
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, uint32_t> graph_cur_after;  // storage buffer holding the state after the graph
   cudaStream_t user_stream = nullptr;  // caller's stream (NULL: the world's own)
-  bool timing = false;
+  uint32_t timing = 0;                 // 0 off, 1 events around every phase, 2 around the contact phase only
+  bool mark_open = false;              // mark_begin recorded a start event that mark_end closes
   float cell_scale = 1.0f;             // cell edge = scale x the smallest exact edge (autotuned)
   // contact recording of the eager path (adjoint recomputation)
   uint32_t* rec_list = nullptr;
@@ -716,6 +729,8 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, const Hos
   d.key = cv.take<uint32_t>(ss);
   d.ckey = cv.take<uint32_t>(ss);
   d.where = cv.take<uint32_t>(ss);
+  d.defer_list = cv.take<uint32_t>(ss);
+  d.defer_count = cv.take<uint32_t>(sorted_storage ? 1u : 0u);
   pos[0] = cv.take<float2>(nb);
   pos[1] = cv.take<float2>(nb);
   d.pos_old = cv.take<float2>(nb);
@@ -768,6 +783,7 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, const Hos
   d.ccount = cv.take<uint8_t>(sorted_storage ? 0u : nc);
   d.bslow = cv.take<uint8_t>(sorted_storage ? 0u : nb);
   d.tile_sums = cv.take<uint32_t>(n_tiles);
+  d.scan_state = cv.take<unsigned long long>((size_t)n_tiles + 1);
   *counters = cv.take<Counters>(1);
 }
 
@@ -781,7 +797,9 @@ namespace {
 enum { PHASE_SCAN = 0, PHASE_SCATTER = 1, PHASE_CONTACT = 2, PHASE_JOINTS = 3, PHASE_INTEGRATE = 4, N_PHASES = 5 };
 
 void mark_begin(blobs_world* w, int phase) {
-  if (!w->recording) return;
+  w->mark_open = false;
+  if (!w->recording || (w->timing == 2 && phase != PHASE_CONTACT)) return;
+  w->mark_open = true;
   TimingSet::Mark m{phase, nullptr, nullptr};
   cudaEventCreate(&m.a);
   cudaEventCreate(&m.b);
@@ -791,7 +809,8 @@ void mark_begin(blobs_world* w, int phase) {
 }
 
 void mark_end(blobs_world* w) {
-  if (!w->recording) return;
+  if (!w->recording || !w->mark_open) return;
+  w->mark_open = false;
   cudaEvent_t b = w->recording->marks.back().b;
   if (w->capturing) cudaEventRecordWithFlags(b, w->st(), cudaEventRecordExternal);
   else cudaEventRecord(b, w->st());
@@ -878,6 +897,11 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.v_out = d.sv[w->v_tracks() ? out : w->vbuf];
     mark_begin(w, coll ? PHASE_CONTACT : PHASE_INTEGRATE);
     launch_step_single(d, a, w->single_mode, st);
+    if (coll && !(a.rec_list || d.ev_rec)) {
+      // the plain step defers bodies with many candidates to a warp each
+      launch_step_deferred(d, a, w->single_mode, st);
+      w->enqueued += 1;
+    }
     mark_end(w);
     if (coll && d.ev_rec) {
       launch_ev_tick(d, st);
@@ -964,7 +988,7 @@ int launch_steady(blobs_world* w, float delta, uint32_t n_steps) {
     w->keys_valid = true;
   }
   // the buffers baked into a graph depend on where the state is now
-  GraphKey key{f2bits(delta), w->cur | ((uint32_t)w->vbuf << 1), n_steps, w->timing ? 1u : 0u};
+  GraphKey key{f2bits(delta), w->cur | ((uint32_t)w->vbuf << 1), n_steps, w->timing};
   auto it = w->graphs.find(key);
   const uint32_t cur0 = w->cur;
   if (it == w->graphs.end()) {
@@ -1218,6 +1242,8 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   d.contacts_total = counters->contacts_total;
   d.pushouts_total = counters->pushouts_total;
   d.contacts_sub = counters->contacts_sub;
+  d.walk_total = counters->walk_total;
+  d.walk_sub = counters->walk_sub;
   d.status = &counters->status;
   w->dcounters = counters;
 
@@ -1298,6 +1324,8 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)h.n_cells, s);
   if (e == cudaSuccess && !sorted_storage) e = cudaMemsetAsync(d.bslow, 0, nb, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(Counters), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.scan_state, 0, sizeof(unsigned long long) * ((size_t)n_tiles + 1), s);
+  if (e == cudaSuccess && sorted_storage) e = cudaMemsetAsync(d.defer_count, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) {
     cudaFree(w->arena);
     w->arena = nullptr;
@@ -1436,6 +1464,16 @@ int blobs_world_pushout_count(blobs_world* w, uint64_t* total) {
   return st;
 }
 
+int blobs_world_walk_count(blobs_world* w, uint64_t* total, uint64_t* last_substep) {
+  if (!w) return BLOBS_ERR_INVALID_HANDLE;
+  if (!w->loaded) return BLOBS_ERR_STATE;
+  cudaSetDevice(w->cfg.device);
+  int st = read_status(w);
+  if (total) *total = w->hcounters->walks();
+  if (last_substep) *last_substep = w->hcounters->walks_sub();
+  return st;
+}
+
 int blobs_world_time(blobs_world* w, double* time, double* accumulator) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
   if (time) *time = w->time;
@@ -1497,6 +1535,9 @@ int blobs_world_restore(blobs_world* w) {
   cudaError_t e = cudaSetDevice(w->cfg.device);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   e = cudaMemcpyAsync(w->arena, w->snap.mem, w->arena_bytes, cudaMemcpyDeviceToDevice, w->st());
+  // the scan's ticket must never run backwards: restart its epochs
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(w->dev.scan_state, 0, sizeof(unsigned long long) * ((size_t)w->dev.n_tiles + 1), w->st());
   if (e != cudaSuccess) return blobs_map_cuda(e);
   w->old_dt = w->snap.old_dt;
   w->v_div = w->snap.v_div;
@@ -1738,8 +1779,8 @@ int blobs_world_backward(blobs_world* w, const float* dl_dpos, float* dl_dvreq, 
   int in = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(adj[in][0], dl_dpos, slice, cudaMemcpyHostToDevice, st);
   const float dt_sub = (float)r.delta / (float)w->cfg.substeps;
-  const bool saved_timing = w->timing;
-  w->timing = false;
+  const uint32_t saved_timing = w->timing;
+  w->timing = 0;
   // the recomputed substeps are not new collisions: no events
   w->dev.ev_rec = nullptr;
   int status = BLOBS_OK;
@@ -2001,7 +2042,8 @@ int blobs_world_kernel_launches(blobs_world* w, uint64_t* count) {
 
 int blobs_world_set_timing(blobs_world* w, int enabled) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
-  w->timing = enabled != 0;
+  if (enabled < 0 || enabled > 2) return BLOBS_ERR_INVALID_ARGUMENT;
+  w->timing = (uint32_t)enabled;
   return BLOBS_OK;
 }
 

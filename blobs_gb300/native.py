@@ -92,6 +92,7 @@ def lib() -> ctypes.CDLL:
         "blobs_world_read_snapshots": (i32, [_P, _P]),
         "blobs_world_contact_count": (i32, [_P, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "blobs_world_pushout_count": (i32, [_P, ctypes.POINTER(u64)]),
+        "blobs_world_walk_count": (i32, [_P, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "blobs_world_time": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "blobs_world_joint_order": (i32, [_P, _P, ctypes.POINTER(u32)]),
         "blobs_world_snapshot": (i32, [_P]),
@@ -329,8 +330,11 @@ class World:
         check(lib().blobs_world_read_bodies(self._h, _ptr(pos), _ptr(pos_old), _ptr(vel), _ptr(rotation),
                                             _ptr(angvel)), "read_bodies")
 
-    def set_timing(self, enabled: bool) -> None:
-        check(lib().blobs_world_set_timing(self._h, 1 if enabled else 0), "set_timing")
+    def set_timing(self, enabled, contact_only: bool = False) -> None:
+        """Per-phase CUDA events in the step graphs (contact_only: around the
+        contact phase alone)."""
+        mode = (2 if contact_only else 1) if enabled else 0
+        check(lib().blobs_world_set_timing(self._h, mode), "set_timing")
 
     def emit_pairs(self, contacts_only: bool, cap: Optional[int] = None):
         """(hi, lo) collider pairs of the broadphase (see blobs_world_emit_pairs),
@@ -422,6 +426,12 @@ class World:
     def contact_count(self):
         t, l = ctypes.c_uint64(), ctypes.c_uint64()
         check(lib().blobs_world_contact_count(self._h, ctypes.byref(t), ctypes.byref(l)), "contact_count")
+        return int(t.value), int(l.value)
+
+    def walk_count(self):
+        """(total, last substep) bodies whose contacts took the selection walk."""
+        t, l = ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().blobs_world_walk_count(self._h, ctypes.byref(t), ctypes.byref(l)), "walk_count")
         return int(t.value), int(l.value)
 
     def pushout_count(self) -> int:

@@ -202,8 +202,9 @@ int blobs_world_restore(blobs_world* w);
  * graph) since it was created. */
 int blobs_world_kernel_launches(blobs_world* w, uint64_t* count);
 
-/* When enabled, CUDA events are recorded around each kernel phase of every
- * substep (inside the step graphs). */
+/* enabled = 1: CUDA events are recorded around each kernel phase of every
+ * substep (inside the step graphs); 2: around the contact phase only (its
+ * kernel timed without event nodes between the other kernels); 0: off. */
 int blobs_world_set_timing(blobs_world* w, int enabled);
 /* Device milliseconds and launch counts per phase since the previous call:
  * [0] cell scan, [1] scatter + forces, [2] contacts (+ fused integration),
@@ -224,6 +225,11 @@ int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_su
 /* Contacts resolved with the coincident-centre push-out branch
  * (physics.rs:272-286) since load. */
 int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
+/* No counterpart in the reference (a cost diagnostic): bodies of the
+ * single-sphere path whose 3x3 cells held too many candidates for the
+ * bit-mask pass, so their contacts took the exact selection walk -- since
+ * load and in the last substep. */
+int blobs_world_walk_count(blobs_world* w, uint64_t* total, uint64_t* last_substep);
 /* The broadphase output for the current collider snapshots: every collider
  * pair (hi, lo), hi > lo in arena order, whose cells are 3x3 neighbours in
  * its world's grid (contacts_only = 0), or only the pairs the contact pass

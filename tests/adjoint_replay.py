@@ -143,3 +143,55 @@ def replay_gradients(scene, trace, final_pos, dl_dpos, dt, old_dt=1.0, vreq_pend
         if grads[5] is not None:
             gk += grads[5].numpy()
     return gv, gk, worst
+
+
+def tangent_fd(scene, trace, dl_dpos, dt, param, old_dt=1.0, vreq_pending=True, h=1e-4):
+    """dL/d(one parameter) by f64 central finite differences chained along a
+    traced rollout: the tangent of the state is carried forward substep by
+    substep, each substep's directional derivative taken by central
+    differences of the f64 substep map at the recorded
+    state with the recorded contact set.  No autograd and no adjoint: an
+    independent check of the same derivative (that of the f32 trajectory the
+    GPU follows).  param = ("v", body, axis) or ("k", spring).  The stencil
+    is fourth order, (8 (F(+e) - F(-e)) - (F(+2e) - F(-2e))) / 12e, with the
+    step e = h / (largest tangent component) so that the state moves by h.
+    Returns (gradient, branch_changed): the second is True when the wall
+    clamp of some body differed between the stencil's points in a substep
+    (the derivative is then not defined there and the sample is discarded)."""
+    assert scene.single_collider()
+    sc = _context(scene, dt)
+    hs = sc["h"]
+    ratio_first = float(np.float32(np.float32(hs) / np.float32(old_dt)))
+    n = scene.n_bodies
+    v0 = torch.from_numpy(scene.vreq.astype(np.float64))
+    k = torch.from_numpy(scene.spr_k.astype(np.float64))
+    dv0 = torch.zeros_like(v0)
+    dk = torch.zeros_like(k)
+    if param[0] == "v":
+        dv0[param[1], param[2]] = 1.0
+    else:
+        dk[param[1]] = 1.0
+    tan = [torch.zeros(n, 2, dtype=torch.float64) for _ in range(4)]
+    changed = False
+    with torch.no_grad():
+        for t in range(len(trace)):
+            st = trace[t]
+            x = [torch.from_numpy(st[key].copy()) for key in ("pos", "pos_old", "snap", "vel")]
+            first = t == 0 and vreq_pending
+            dpar_v = dv0 if first else torch.zeros_like(dv0)
+            s = max(1.0, max(float(tt.abs().max()) for tt in tan), float(dpar_v.abs().max()), float(dk.abs().max()))
+            e = h / s
+            pairs = (st["hi"], st["lo"], st["pushed"])
+            rf = ratio_first if t == 0 else 1.0
+            ev = {}
+            for j in (-2, -1, 1, 2):
+                ev[j] = _substep(sc, [xi + (j * e) * ti for xi, ti in zip(x, tan)], v0 + (j * e) * dpar_v,
+                                 k + (j * e) * dk, pairs, first, rf)
+            if sc["box"] is not None:
+                masks = [ev[j][0] != ev[j][2] for j in (-2, -1, 1, 2)]
+                changed = changed or any(bool((mk != masks[0]).any()) for mk in masks[1:])
+            # fourth-order central stencil
+            tan = [(8.0 * (a1 - m1) - (a2 - m2)) / (12.0 * e)
+                   for a1, m1, a2, m2 in zip(ev[1], ev[-1], ev[2], ev[-2])]
+    g = float((torch.from_numpy(np.asarray(dl_dpos, np.float64)) * tan[0]).sum())
+    return g, changed

@@ -11,8 +11,13 @@ the f32 GPU adjoint, checked two ways:
 * against f64 central finite differences of the oracle (h = 1e-4 for
   velocities, 1e-4 relative for stiffnesses) over horizons of two and four
   steps, where the f32 and f64 trajectories still resolve the same contacts:
-  within 1e-3 relative (or 1e-5 of the largest gradient of the kind); a
-  sample whose contact count changes within +-h is discarded.
+  within 2e-3 relative (or 2e-7 of the largest gradient of the kind); a
+  sample whose contact count changes within +-h is discarded and replaced;
+* on the full differentiable-rollout batch with a checkpoint every 16 steps
+  over 17, 24 and 33 steps (one and two checkpoints restored): against the
+  replay, and against f64 central differences chained along the traced
+  trajectory (adjoint_replay.tangent_fd), which need neither autograd nor
+  the f64 oracle's own, diverging, trajectory.
 
 Over longer horizons the f32 and f64 trajectories drift apart by ~1e-4 and
 resolve different contacts, and the derivative of the contact correction
@@ -25,7 +30,7 @@ import pytest
 from blobs_gb300 import native, scenes
 from oracle import oracle
 
-from adjoint_replay import replay_gradients
+from adjoint_replay import replay_gradients, tangent_fd
 
 pytestmark = pytest.mark.gpu
 
@@ -76,10 +81,10 @@ def gpu_gradients(scene, marked, targets, steps, every, warm_steps=0):
     return final, g, after, gv.astype(np.float64), gk.astype(np.float64)
 
 
-def _close(got, want, what):
+def _close(got, want, what, floor=1e-4):
     scale = np.abs(want).max()
     err = np.abs(got - want)
-    bad = err > 1e-3 * np.abs(want) + 1e-4 * scale
+    bad = err > 1e-3 * np.abs(want) + floor * scale
     assert not bad.any(), (what, int(bad.sum()), float(err.max()), float(scale))
 
 
@@ -185,10 +190,10 @@ def test_gradients_match_f64_finite_differences(steps):
         o64.step(scene.dt, steps)
         same.append(o32.contacts == o64.contacts)
     assert any(same)
-    floor_v, floor_k = 1e-2 * np.abs(gv).max(), 1e-2 * np.abs(gk).max()
+    floor_v, floor_k = 1e-4 * np.abs(gv).max(), 1e-4 * np.abs(gk).max()
     rng = np.random.Generator(np.random.PCG64(99))
-    checked, discarded = 0, 0
-    for trial in range(64):
+    checked, discarded, worst = 0, 0, 0.0
+    for trial in range(256):
         if checked >= 32:
             break
         if trial % 2 == 0:
@@ -224,9 +229,15 @@ def test_gradients_match_f64_finite_differences(steps):
             discarded += 1
             continue
         fd = (Lp - Lm) / (2.0 * h)
-        assert abs(g_gpu - fd) <= 1e-3 * max(abs(fd), floor), (trial, g_gpu, fd)
+        # the f64 trajectory is not the f32 one the GPU differentiates: at two
+        # and four steps they differ by ~1e-6, which moves small gradients by
+        # up to ~1.5e-3 of themselves
+        err = abs(g_gpu - fd) / (2e-3 * max(abs(fd), floor))
+        worst = max(worst, err)
+        assert err <= 1.0, (trial, g_gpu, fd, floor)
         checked += 1
-    assert checked >= 16, (checked, discarded)
+    assert checked == 32, (checked, discarded)
+    print("steps %d: 32 samples within %.3g of the bound, %d discarded" % (steps, worst, discarded))
 
 
 def test_zero_loss_weight_gives_zero_gradients():
@@ -346,3 +357,67 @@ def test_backward_is_deterministic():
     _, _, _, gv, gk = gpu_gradients(scene, marked, targets, 8, 3)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(a[0].astype(np.float64), gv) and np.array_equal(a[1].astype(np.float64), gk)
+
+
+@pytest.mark.parametrize("steps", [17, 24, 33])
+def test_gradient_batch_across_checkpoints_matches_finite_differences(steps):
+    """The differentiable-rollout batch at full size (256 worlds x 2,048
+    spheres, 1,024 springs per world, 64 marked bodies) with a checkpoint
+    every 16 steps, over 17, 24 and 33 steps: the backward pass restores one
+    or two checkpoints and recomputes their segments.  Worlds 0 and 255 are
+    checked (1) in full against the f64 replay of the traced f32 oracle, and
+    (2) at 32 sampled parameters (velocities and stiffnesses alternating)
+    against f64 central finite differences chained along the same traced
+    trajectory (adjoint_replay.tangent_fd: fourth-order stencil per substep,
+    state step 1e-3, recorded contact sets), within 1e-3 relative with a
+    floor of 1e-4 of the largest gradient of the kind in that world; a
+    sample whose wall clamp changes inside the stencil is discarded and
+    reported.  Finite differences of the f64 oracle from the initial state
+    are no reference here: on these overlapping starts the f32 and f64
+    trajectories are 0.5 units apart after 17 steps."""
+    scene, marked, targets = scenes.gradient_batch()
+    final, g, after, gv, gk = gpu_gradients(scene, marked, targets, steps, 16)
+    assert np.array_equal(final, after)
+    assert np.all(np.isfinite(gv)) and np.all(np.isfinite(gk))
+    rng = np.random.Generator(np.random.PCG64(1000 + steps))
+    checked, discarded, worst = 0, 0, 0.0
+    for w in (0, scene.n_worlds - 1):
+        sub = scenes.unpack_world(scene, w)
+        b0, b1 = int(scene.world_body_offsets[w]), int(scene.world_body_offsets[w + 1])
+        s0, s1 = int(scene.world_spring_offsets[w]), int(scene.world_spring_offsets[w + 1])
+        o = oracle.OracleWorld(sub, 32)
+        o.trace(True)
+        assert o.step(scene.dt, steps) == 0
+        assert o.pushouts == 0
+        fin = o.bodies()["pos"]
+        assert np.array_equal(fin.astype(np.float32), final[b0:b1].astype(np.float32)), w
+        tr = o.traced()
+        rv, rk, rworst = replay_gradients(sub, tr, fin, g[b0:b1], scene.dt)
+        _check_replay(rworst, fin)
+        # the f32 adjoint's own rounding, amplified along the horizon: within
+        # 1e-4 of the largest gradient up to 24 steps, 3e-4 at 33
+        floor = 1e-4 if steps <= 24 else 3e-4
+        _close(gv[b0:b1], rv, ("dL/dv0", w, steps), floor)
+        _close(gk[s0:s1], rk, ("dL/dk", w, steps), floor)
+        wv, wk = gv[b0:b1], gk[s0:s1]
+        floor_v, floor_k = 1e-4 * np.abs(wv).max(), 1e-4 * np.abs(wk).max()
+        n_here = 0
+        while n_here < 16:
+            if n_here % 2 == 0:
+                b, ax = divmod(_pick(rng, wv.reshape(-1)), 2)
+                param, g_gpu, floor = ("v", b, ax), wv[b, ax], floor_v
+            else:
+                e = _pick(rng, wk)
+                param, g_gpu, floor = ("k", e), wk[e], floor_k
+            fd, changed = tangent_fd(sub, tr, g[b0:b1], scene.dt, param)
+            if changed:
+                discarded += 1
+                assert discarded <= 16, discarded
+                continue
+            err = abs(g_gpu - fd) / (1e-3 * max(abs(fd), floor))
+            worst = max(worst, err)
+            assert err <= 1.0, (w, param, g_gpu, fd, floor)
+            n_here += 1
+            checked += 1
+    assert checked == 32
+    print("steps %d: 32 samples within %.3g of the bound, %d discarded" % (steps, worst, discarded))
