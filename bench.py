@@ -5,7 +5,7 @@ packing with overlaps, walled box, seeded synthetic scene, 1,000-step
 rollout).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --section general|batched [--steps K] [--warmup W]
+  python bench.py --section general|batched|dense [--steps K] [--warmup W]
 
 One JSON line on rank 0.  The whole 1,000-step rollout runs from t = 0,
 every step between its own CUDA-event pair on the world's stream with L2
@@ -259,7 +259,8 @@ def run_section(args):
     import torch
     from blobs_gb300 import native, scenes
     scene = {"general": lambda: scenes.jointed_bodies(),
-             "batched": lambda: scenes.uneven_batch()}[args.section]()
+             "batched": lambda: scenes.uneven_batch(),
+             "dense": lambda: scenes.dense_spheres(n=args.n, packing=0.8)}[args.section]()
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
@@ -287,10 +288,13 @@ def run_section(args):
         e1.record(stream)
         torch.cuda.synchronize()
         ms += e0.elapsed_time(e1)
+    contacts_last = w.contact_count()[1]
+    walk_last = w.walk_count()[1] if scene.single_collider() else None
     w.close()
     print(json.dumps({"section": args.section, "bodies": scene.n_bodies, "colliders": scene.n_colliders,
                       "worlds": scene.n_worlds, "steps": args.steps, "warmup": args.warmup,
-                      "ms_per_step": ms / args.steps,
+                      "ms_per_step": ms / args.steps, "contacts_last_substep": contacts_last,
+                      "deferred_bodies_last_substep": walk_last,
                       "phase_us_per_substep": {k: 1e3 * v / args.steps / scene.substeps for k, v in phase.items()}}),
           flush=True)
 
@@ -766,8 +770,9 @@ def main():
     ap.add_argument("--no-general", action="store_true")
     ap.add_argument("--no-literal", action="store_true", help="skip the 2000 x 2000 literal-box run")
     ap.add_argument("--no-sparse", action="store_true", help="skip the 1,000-sphere full-run comparison")
-    ap.add_argument("--section", choices=["general", "batched"], default=None,
-                    help="run one secondary workload alone (profiling driver), print its phase times")
+    ap.add_argument("--section", choices=["general", "batched", "dense"], default=None,
+                    help="run one secondary workload alone (profiling driver), print its phase times; dense: the "
+                         "1M-sphere world at 80%% packing, the density of the rollout's settled pile")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
