@@ -23,7 +23,7 @@ enum : uint8_t {
 // Device status bits, read back by the host after a synchronising call.
 enum : uint32_t {
   ST_NAN = 1u,         // NaN contact normal or non-finite rotation (physics.rs:293, 471-474)
-  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (the single-pass scan's look-back)
+  ST_TIMEOUT = 2u,     // a bounded spin-wait gave up (reserved: no kernel waits on another)
   ST_BAD_INDEX = 4u,   // a device bounds check fired
 };
 
@@ -121,10 +121,6 @@ struct WorldDev {
   uint8_t* ccount;           // general path, per collider: contacts in clist
   uint8_t* bslow;            // general path, per body: contacts need the ordered walk (zero between substeps)
   uint32_t* tile_sums;       // per scan tile
-  // single-pass scan (NULL: the two-kernel scan): [0] the tile ticket,
-  // [1 + t] tile t's published value: (epoch * 4 + state) << 32 | sum, state
-  // 1 = the tile's own sum, 2 = the sum of every tile up to and including it
-  unsigned long long* scan_state;
 
   // single-sphere path: body storage re-sorted into cell order once per step
   float4* sa[2];             // (snapshot x, y, radius, arena id bits), double-buffered per substep
@@ -304,7 +300,6 @@ __device__ __forceinline__ void record_event(const WorldDev& w, uint32_t a, uint
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // polls of a predecessor tile before ST_TIMEOUT
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
 constexpr uint32_t CL_CAP = 8;             // general path: contacts kept per collider
 constexpr uint32_t COUNTER_BINS = 64;

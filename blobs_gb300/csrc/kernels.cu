@@ -165,137 +165,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(WorldDev w) {
   }
 }
 
-// Single-pass scan (decoupled look-back): each block takes the next tile
-// ticket, publishes its tile's sum, then sums the published values of the
-// tiles before it -- walking back until one publishes its inclusive prefix
-// -- and publishes its own inclusive prefix.  A block only waits on tiles
-// whose tickets were taken earlier (so whose blocks are running), and every
-// wait is bounded: after SCAN_SPIN_LIMIT polls it sets ST_TIMEOUT and goes
-// on with what it has (the host then reports BLOBS_ERR_TIMEOUT).  Published
-// values carry the launch's epoch (ticket / tiles), so the state needs no
-// reset between launches.
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_onepass(WorldDev w) {
-  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
-  __shared__ uint32_t s_tile, s_epoch, s_prefix;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t tiles = w.n_tiles;
-  if (threadIdx.x == 0) {
-    const unsigned long long tk = atomicAdd(w.scan_state, 1ull);
-    s_tile = (uint32_t)(tk % tiles);
-    s_epoch = (uint32_t)((tk / tiles) & 0x3fffffffull);
-  }
-  if (blockIdx.x == 0 && threadIdx.x < COUNTER_BINS) {
-    if (w.contacts_sub) w.contacts_sub[threadIdx.x] = 0u;
-    if (w.walk_sub) w.walk_sub[threadIdx.x] = 0u;
-    if (threadIdx.x == 0 && w.defer_count) *w.defer_count = 0u;
-  }
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const unsigned long long tag = (unsigned long long)(s_epoch * 4u) << 32;
-  unsigned long long* flags = w.scan_state + 1;
-  const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
-  uint32_t v[SCAN_ITEMS];
-  load_tile(w, base, v, true);
-  uint32_t tsum = 0;
-#pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) tsum += v[i];
-  // exclusive scan of the thread sums across the block
-  uint32_t x = tsum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= (uint32_t)o) x += y;
-  }
-  if (lane == 31) s_warp[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int NW = SCAN_THREADS / 32;
-    uint32_t t = lane < NW ? s_warp[lane] : 0u;
-#pragma unroll
-    for (int o = 1; o < NW; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= (uint32_t)o) t += y;
-    }
-    if (lane < NW) s_warp[lane] = t;
-    const uint32_t agg = __shfl_sync(0xffffffffu, t, NW - 1);
-    // publish the tile's own sum (or, for tile 0, its inclusive prefix)
-    if (lane == 0) st_release_u64(flags + tile, tag | ((unsigned long long)(tile ? 1u : 2u) << 32) | agg);
-    // look back
-    uint32_t prefix = 0;
-    int pred = (int)tile - 1;
-    uint32_t polls = 0;
-    bool timed_out = false;
-    while (pred >= 0) {
-      const int t2 = pred - (int)lane;
-      unsigned long long f = 0ull;
-      uint32_t state = 2u;  // before tile 0: an inclusive prefix of 0
-      if (t2 >= 0) {
-        f = ld_acquire_u64(flags + t2);
-        const uint32_t hi = (uint32_t)(f >> 32);
-        state = (hi & ~3u) == (s_epoch * 4u) ? (hi & 3u) : 0u;
-      }
-      const uint32_t incl = __ballot_sync(0xffffffffu, state == 2u);
-      const uint32_t ready = __ballot_sync(0xffffffffu, state != 0u);
-      const uint32_t first = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;  // the window ends at the first inclusive
-      const uint32_t need = first == 31u ? 0xffffffffu : ((2u << first) - 1u);
-      if ((ready & need) != need) {
-        if (++polls >= SCAN_SPIN_LIMIT) {  // bounded: give up, report, finish
-          timed_out = true;
-          break;
-        }
-        __nanosleep(32);
-        continue;
-      }
-      uint32_t add = (lane <= first) ? (uint32_t)f : 0u;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(0xffffffffu, add, o);
-      prefix += add;
-      if (incl) break;
-      pred -= 32;
-    }
-    if (lane == 0) {
-      if (timed_out) atomicOr(w.status, ST_TIMEOUT);
-      if (tile) st_release_u64(flags + tile, tag | (2ull << 32) | (uint32_t)(prefix + agg));
-      s_prefix = prefix;
-    }
-  }
-  __syncthreads();
-  uint32_t run = s_prefix + (warp ? s_warp[warp - 1] : 0u) + x - tsum;
-  const uint32_t n = w.n_cells;
-  if (base + SCAN_ITEMS <= n) {
-    uint4* dst = reinterpret_cast<uint4*>(w.cell_start + base);
-#pragma unroll
-    for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
-      uint4 t;
-      t.x = run; run += v[4 * q + 0];
-      t.y = run; run += v[4 * q + 1];
-      t.z = run; run += v[4 * q + 2];
-      t.w = run; run += v[4 * q + 3];
-      dst[q] = t;
-    }
-    if (base + SCAN_ITEMS == n) w.cell_start[n] = run;
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-      const size_t k = base + i;
-      if (k < n) {
-        w.cell_start[k] = run;
-        run += v[i];
-        if (k + 1 == n) w.cell_start[n] = run;
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // gravity + springs for one body (physics.rs:369-375, springs.rs:25-47,
 // rigid_body.rs:155-160).  Springs are visited in ascending arena index and
@@ -1114,10 +983,6 @@ void launch_keys(const WorldDev& w, bool mw, cudaStream_t st) {
 
 void launch_scan(const WorldDev& w, cudaStream_t st) {
   const uint32_t tiles = blocks_for(w.n_cells, SCAN_TILE);
-  if (w.scan_state && tiles == w.n_tiles) {
-    k_scan_onepass<<<tiles, SCAN_THREADS, 0, st>>>(w);
-    return;
-  }
   k_tile_sums<<<tiles, SCAN_THREADS, 0, st>>>(w);
   k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(w);
 }

@@ -261,24 +261,7 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
   return p;
 }
 
-// The warp's candidate tests, spread over its lanes.  Every lane (body) has
-// its 3 row ranges of candidates; the warp lists all (body, candidate) pairs
-// body by body (rows in order, candidates ascending), and in each round its
-// 32 lanes test 32 consecutive pairs of that list, so every lane does the
-// same work however unevenly the candidates fall on the bodies.  The near
-// bits come back as one 32-bit word per round; each body then reads its own
-// bits.  Per warp in shared memory: the bodies' records and their row
-// offsets into the pair list, the owner (lane) of every pair, the words.
-constexpr uint32_t COOP_PAIRS = 1024;  // pairs per warp; a warp with more takes the per-lane pass
 constexpr int STEP_THREADS = 256;
-
-struct CoopWarp {
-  float4 body[32];                     // snapshot x, y, radius, arena id bits
-  int4 geo[32];                        // position - pair index for rows 0, 1, 2; first pair of row 1
-  int row2[32];                        // first pair of row 2
-  uint32_t words[COOP_PAIRS / 32 + 2]; // near bits of the pair list
-  uint8_t owner[COOP_PAIRS];           // lane of each pair
-};
 
 // Bodies with more near candidates than this take k_step_deferred.
 constexpr uint32_t DEFER_NEAR = 12;
@@ -456,127 +439,55 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 }
 
 // HOOKS: compiled with the adjoint's contact recording and the collision
-// event stream (the plain step leaves their branches out, and spreads its
-// candidate tests over the warp's lanes).
+// event stream.  The plain step (no hooks) leaves a body whose 3x3 cells
+// hold too many candidates for its near mask, or which has more than
+// DEFER_NEAR near candidates, to k_step_deferred: one such body would hold
+// its whole warp in the O(contacts x candidates) walk or the O(near^2)
+// ordered selection.
 template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, SingleArgs a) {
-  constexpr bool COOP = !HOOKS;
-  __shared__ CoopWarp coop_smem[COOP ? STEP_THREADS / 32 : 1];
+  constexpr bool DEFER = !HOOKS;
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
-  const bool active = j < w.n_bodies;
   uint32_t ncontacts = 0, npush = 0;
   bool walked = false;
   bool deferred = false;  // contacts (and the rest of the body's substep) left to k_step_deferred
-
-  float4 av = make_float4(0.f, 0.f, 0.f, 0.f), bv = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t c = 0;
-  if (active) {
-    av = a.a_in[j];
-    bv = a.b_in[j];
-    c = __float_as_uint(av.w);
+  if (j < w.n_bodies) {
+    const float4 av = a.a_in[j];
+    const float4 bv = a.b_in[j];
+    uint32_t c = __float_as_uint(av.w);
     if (c >= w.n_bodies) {
       atomicOr(w.status, ST_BAD_INDEX);
       c = 0;
     }
-  }
-  const float2 s = v2(av.x, av.y);
-  const float r = av.z;
-  const WorldParam wp0 = w.wparam[0];
-  const BodyConst k = body_const<MODE>(w, wp0, c, r);
-  const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
-
-  // the 3 candidate rows of a body away from the grid edge: contiguous
-  // ranges of the cell-order array
-  const uint32_t own_key = (active && a.contacts) ? a.own_cell[j] : 0u;
-  const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
-  const uint32_t lx = (own_key - wp.cell_base) & wm, ly = (own_key - wp.cell_base) >> wp.log2w;
-  const bool interior = active && a.contacts && lx >= 1u && lx < wm && ly >= 1u && ly < hm;
-  uint32_t s0 = 0, s1 = 0, s2 = 0, l0 = 0, l1 = 0, l2 = 0;
-  if (interior) {
-    const uint32_t n = w.n_bodies;
-    const uint32_t r1 = own_key - 1u, r0 = r1 - (wm + 1u), r2 = r1 + (wm + 1u);
-    s0 = w.cell_start[r0];
-    s1 = w.cell_start[r1];
-    s2 = w.cell_start[r2];
-    const uint32_t e0 = min(w.cell_start[r0 + 3u], n), e1 = min(w.cell_start[r1 + 3u], n),
-                   e2 = min(w.cell_start[r2 + 3u], n);
-    l0 = e0 > s0 ? e0 - s0 : 0u;
-    l1 = e1 > s1 ? e1 - s1 : 0u;
-    l2 = e2 > s2 ? e2 - s2 : 0u;
-  }
-
-  // Phase 1, spread over the warp (plain steps): near bits of every body
-  // whose rows hold at most 64 candidates.
-  unsigned long long near = 0ull;
-  bool coop_done = false;
-  if (COOP && a.contacts) {
-    const uint32_t tot = l0 + l1 + l2;
-    const uint32_t nl = (interior && tot <= 64u) ? tot : 0u;
-    uint32_t incl = nl;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= (uint32_t)o) incl += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    const uint32_t off = incl - nl;
-    if (total <= COOP_PAIRS) {  // warp-uniform
-      CoopWarp& S = coop_smem[COOP ? (threadIdx.x >> 5) : 0];
-      S.body[lane] = make_float4(s.x, s.y, r, av.w);
-      S.geo[lane] = make_int4((int)s0 - (int)off, (int)s1 - (int)(off + l0), (int)s2 - (int)(off + l0 + l1),
-                              (int)(off + l0));
-      S.row2[lane] = (int)(off + l0 + l1);
-      for (uint32_t t = 0; t < nl; ++t) S.owner[off + t] = (uint8_t)lane;
-      __syncwarp();
-      const float4* __restrict__ C = a.cand;
-      for (uint32_t base = 0; base < total; base += 32u) {
-        const uint32_t q = base + lane;
-        bool nr = false;
-        if (q < total) {
-          const uint32_t ow = S.owner[q];
-          const float4 ob = S.body[ow];
-          const int4 g = S.geo[ow];
-          const int pq = (int)q;
-          const int d = pq < g.w ? g.x : (pq < S.row2[ow] ? g.y : g.z);
-          const float4 o = C[pq + d];
-          nr = near_pair(ob.x - o.x, ob.y - o.y, ob.z + o.z) && __float_as_uint(o.w) != __float_as_uint(ob.w);
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, nr);
-        if (lane == 0) S.words[base >> 5] = bal;
-      }
-      __syncwarp();
-      if (nl) {
-        const uint32_t w0 = off >> 5, sh = off & 31u;
-        const unsigned long long lo = (unsigned long long)S.words[w0] | ((unsigned long long)S.words[w0 + 1] << 32);
-        near = lo >> sh;
-        if (sh) near |= (unsigned long long)S.words[w0 + 2] << (64u - sh);
-        if (nl < 64u) near &= (1ull << nl) - 1ull;
-        coop_done = true;
-      }
-      __syncwarp();  // the warp's next use of S (none in this launch) comes after every read
-    }
-  }
-
-  if (active) {
+    const float2 s = v2(av.x, av.y);
+    const float r = av.z;
+    const WorldParam wp0 = w.wparam[0];
+    const BodyConst k = body_const<MODE>(w, wp0, c, r);
+    const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
     const float2 p0 = v2(bv.x, bv.y);  // position at the start of the substep
     float2 p = p0;
     uint32_t nrec = 0;  // contacts recorded for the adjoint
 
-    if (COOP && coop_done) {
-      // Phase 2 on the warp's near bits (rows at bits 0, l0, l0 + l1); a
-      // body with many near candidates is left to a warp of its own
-      if (__popcll(near) > DEFER_NEAR) deferred = true;
-      else
-        p = apply_near<MODE, HOOKS>(w, a, near, s0, s1, s2, l0, l0 + l1, j, c, p0, s, r, k.m, ncontacts, npush,
-                                    nrec);
-    } else if (interior) {
+    const uint32_t own_key = a.contacts ? a.own_cell[j] : 0u;
+    const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
+    const uint32_t lx = (own_key - wp.cell_base) & wm, ly = (own_key - wp.cell_base) >> wp.log2w;
+    const bool interior = lx >= 1u && lx < wm && ly >= 1u && ly < hm;
+    if (a.contacts && interior) {
+      // Cells away from the grid edge: the 3x3 block is three contiguous
+      // ranges of the cell-order array, one per row.
+      const float4* __restrict__ C = a.cand;
+      const uint32_t n = w.n_bodies;
+      const uint32_t r1 = own_key - 1u, r0 = r1 - (wm + 1u), r2 = r1 + (wm + 1u);
+      const uint32_t s0 = w.cell_start[r0], s1 = w.cell_start[r1], s2 = w.cell_start[r2];
+      const uint32_t e0 = min(w.cell_start[r0 + 3u], n), e1 = min(w.cell_start[r1 + 3u], n),
+                     e2 = min(w.cell_start[r2 + 3u], n);
+      const uint32_t l0 = e0 > s0 ? e0 - s0 : 0u, l1 = e1 > s1 ? e1 - s1 : 0u, l2 = e2 > s2 ? e2 - s2 : 0u;
       // bit positions are padded to multiples of 4 per row: they must fit 64
       if (((l0 + 3u) & ~3u) + ((l1 + 3u) & ~3u) + ((l2 + 3u) & ~3u) <= 64u) {
-        // Phase 1 per lane: squared-distance test per candidate (self
-        // excluded); near candidates become bits of their position (row 0
-        // at bit 0, row 1 at bit 4*ceil(l0/4), ...).
-        const float4* __restrict__ C = a.cand;
+        // Phase 1: squared-distance test per candidate (self excluded); near
+        // candidates become bits of their position (row 0 at bit 0, row 1
+        // at bit 4*ceil(l0/4), ...).
         unsigned long long nb = 0ull;
         uint32_t t = 0;
         near_range(C, s, r, c, s0, s0 + l0, t, nb);
@@ -584,8 +495,10 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, Sin
         near_range(C, s, r, c, s1, s1 + l1, t, nb);
         const uint32_t t2 = t;
         near_range(C, s, r, c, s2, s2 + l2, t, nb);
-        p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
-      } else if (COOP) {
+        // Phase 2: the near candidates in ascending arena id
+        if (DEFER && __popcll(nb) > DEFER_NEAR) deferred = true;
+        else p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+      } else if (DEFER) {
         deferred = true;
       } else {
         p = contacts_walk<MODE, HOOKS>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
@@ -639,7 +552,7 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, Sin
             if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
           }
         }
-      } else if (COOP) {
+      } else if (DEFER) {
         deferred = true;
       } else {
         p = contacts_walk<MODE, HOOKS>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
@@ -651,10 +564,9 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, Sin
       a.rec_n[c] = nrec;
       if (nrec) atomicMax(a.rec_max, nrec);
     }
-
     if (!deferred) finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
   }
-  if (COOP && a.contacts) {
+  if (DEFER && a.contacts) {
     // append the deferred bodies to the list k_step_deferred works through
     const uint32_t dm = __ballot_sync(0xffffffffu, deferred);
     if (dm) {

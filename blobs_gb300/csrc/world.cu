@@ -783,7 +783,6 @@ void carve(Carver& cv, WorldDev& d, float2** pos, Counters** counters, const Hos
   d.ccount = cv.take<uint8_t>(sorted_storage ? 0u : nc);
   d.bslow = cv.take<uint8_t>(sorted_storage ? 0u : nb);
   d.tile_sums = cv.take<uint32_t>(n_tiles);
-  d.scan_state = cv.take<unsigned long long>((size_t)n_tiles + 1);
   *counters = cv.take<Counters>(1);
 }
 
@@ -1324,7 +1323,6 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)h.n_cells, s);
   if (e == cudaSuccess && !sorted_storage) e = cudaMemsetAsync(d.bslow, 0, nb, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(Counters), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d.scan_state, 0, sizeof(unsigned long long) * ((size_t)n_tiles + 1), s);
   if (e == cudaSuccess && sorted_storage) e = cudaMemsetAsync(d.defer_count, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) {
     cudaFree(w->arena);
@@ -1535,9 +1533,6 @@ int blobs_world_restore(blobs_world* w) {
   cudaError_t e = cudaSetDevice(w->cfg.device);
   if (e != cudaSuccess) return blobs_map_cuda(e);
   e = cudaMemcpyAsync(w->arena, w->snap.mem, w->arena_bytes, cudaMemcpyDeviceToDevice, w->st());
-  // the scan's ticket must never run backwards: restart its epochs
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(w->dev.scan_state, 0, sizeof(unsigned long long) * ((size_t)w->dev.n_tiles + 1), w->st());
   if (e != cudaSuccess) return blobs_map_cuda(e);
   w->old_dt = w->snap.old_dt;
   w->v_div = w->snap.v_div;
