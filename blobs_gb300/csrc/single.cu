@@ -406,6 +406,52 @@ __device__ __forceinline__ void finish_single(const WorldDev& w, const SingleArg
   }
 }
 
+
+// Phase 2 of the plain step (at most DEFER_NEAR near candidates): the near
+// candidates' ids are gathered into this thread's shared-memory slots first
+// (independent loads), then the ascending-id selection runs over shared
+// memory and only the chosen candidate's record is loaded again.
+template <int MODE>
+__device__ __forceinline__ float2 apply_near_s(const WorldDev& w, const SingleArgs& a, unsigned long long near,
+                                               uint32_t s0, uint32_t s1, uint32_t s2, uint32_t t1, uint32_t t2,
+                                               uint32_t c, float2 p0, float2 s, float r, float m,
+                                               uint32_t& ncontacts, uint32_t& npush, uint32_t* ids, uint32_t* qs) {
+  const float4* __restrict__ C = a.cand;
+  const uint32_t* __restrict__ Cw = reinterpret_cast<const uint32_t*>(a.cand);
+  float2 p = p0;
+  uint32_t kk = 0;
+  for (unsigned long long mk = near; mk; mk &= mk - 1ull, ++kk) {
+    const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
+    const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
+    ids[kk * STEP_THREADS] = Cw[4u * q + 3u];
+    qs[kk * STEP_THREADS] = q;
+  }
+  uint32_t used = 0u;
+  for (uint32_t it = 0; it < kk; ++it) {
+    uint32_t best = 0xffffffffu, bi = 0u;
+    for (uint32_t i = 0; i < kk; ++i) {
+      const uint32_t id = ids[i * STEP_THREADS];
+      if (!((used >> i) & 1u) && id < best) {
+        best = id;
+        bi = i;
+      }
+    }
+    used |= 1u << bi;
+    if (best >= w.n_bodies || best == c) continue;
+    const float4 bo = C[qs[bi * STEP_THREADS]];
+    const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
+    SinglePair sp;
+    if (!single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
+    if (sp.pushed) p = add(p, sp.push);
+    p = add(p, sp.corr);
+    if (best < c) {
+      ++ncontacts;
+      npush += sp.pushed ? 1u : 0u;
+    }
+  }
+  return p;
+}
+
 // Storage slot i -> its position in this substep's cell order.
 __global__ void __launch_bounds__(256) k_permute(WorldDev w, SingleArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -447,6 +493,9 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, SingleArgs a) {
   constexpr bool DEFER = !HOOKS;
+  // phase 2 slots of the plain step: near candidate ids and positions,
+  // thread-interleaved
+  __shared__ uint32_t s_ids[DEFER ? DEFER_NEAR * STEP_THREADS : 1], s_qs[DEFER ? DEFER_NEAR * STEP_THREADS : 1];
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t ncontacts = 0, npush = 0;
@@ -497,6 +546,8 @@ __global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, Sin
         near_range(C, s, r, c, s2, s2 + l2, t, nb);
         // Phase 2: the near candidates in ascending arena id
         if (DEFER && __popcll(nb) > DEFER_NEAR) deferred = true;
+        else if (DEFER) p = apply_near_s<MODE>(w, a, nb, s0, s1, s2, t1, t2, c, p0, s, r, k.m, ncontacts, npush,
+                                                 s_ids + threadIdx.x, s_qs + threadIdx.x);
         else p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
       } else if (DEFER) {
         deferred = true;
