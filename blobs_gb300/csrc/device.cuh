@@ -300,6 +300,7 @@ __device__ __forceinline__ void record_event(const WorldDev& w, uint32_t a, uint
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SCAN_PREFIX_TILES = 256;  // more tiles: their prefix by one k_tile_prefix block
 constexpr int CONTACT_LIST = 24;           // per-body sorted contact list kept in registers
 constexpr uint32_t CL_CAP = 8;             // general path: contacts kept per collider
 constexpr uint32_t COUNTER_BINS = 64;

@@ -42,7 +42,8 @@ __device__ __forceinline__ WorldParam load_wparam(const WorldDev& w, uint32_t wo
 // ---------------------------------------------------------------------------
 // Cell scan in two wait-free kernels: k_tile_sums reduces each tile of
 // SCAN_TILE cell counts; k_scan_apply gives every tile its prefix by summing
-// the sums of all earlier tiles (at most a few thousand), then writes
+// the sums of all earlier tiles (with more than SCAN_PREFIX_TILES tiles,
+// k_tile_prefix computes those prefixes once, in between), then writes
 // cell_start[k] = sum(cell_count[0..k)), cell_start[n] = total, and resets
 // cell_count to zero for the next substep.
 // ---------------------------------------------------------------------------
@@ -101,14 +102,57 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(WorldDev w) {
   }
 }
 
+// Many tiles (large or batched grids): one block turns the tile sums into
+// their exclusive prefix in place, so that k_scan_apply reads its prefix
+// instead of summing all earlier tiles (quadratic in the tile count).
+__global__ void __launch_bounds__(1024) k_tile_prefix(WorldDev w) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_carry;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_carry = 0u;
+  __syncthreads();
+  for (uint32_t base = 0; base < w.n_tiles; base += 1024u) {
+    const uint32_t t = base + threadIdx.x;
+    const uint32_t v = t < w.n_tiles ? w.tile_sums[t] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t u = s_warp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
+        if (lane >= (uint32_t)o) u += y;
+      }
+      s_warp[lane] = u;
+    }
+    __syncthreads();
+    const uint32_t carry = s_carry;
+    if (t < w.n_tiles) w.tile_sums[t] = carry + (warp ? s_warp[warp - 1] : 0u) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry = carry + s_warp[31];
+    __syncthreads();
+  }
+}
+
+template <bool PREFIXED>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(WorldDev w) {
   __shared__ uint32_t s_warp[SCAN_THREADS / 32];
   __shared__ uint32_t s_prefix;
-  // prefix of this tile = sum of the sums of tiles [0, blockIdx.x)
-  uint32_t p = 0;
-  for (uint32_t t = threadIdx.x; t < blockIdx.x; t += SCAN_THREADS) p += w.tile_sums[t];
-  p = block_sum(p, s_warp);
-  if (threadIdx.x == 0) s_prefix = p;
+  if (PREFIXED) {
+    if (threadIdx.x == 0) s_prefix = w.tile_sums[blockIdx.x];
+  } else {
+    // prefix of this tile = sum of the sums of tiles [0, blockIdx.x)
+    uint32_t p = 0;
+    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += SCAN_THREADS) p += w.tile_sums[t];
+    p = block_sum(p, s_warp);
+    if (threadIdx.x == 0) s_prefix = p;
+  }
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS];
@@ -981,10 +1025,16 @@ void launch_keys(const WorldDev& w, bool mw, cudaStream_t st) {
   else k_keys<false><<<g, 256, 0, st>>>(w);
 }
 
-void launch_scan(const WorldDev& w, cudaStream_t st) {
+uint32_t launch_scan(const WorldDev& w, cudaStream_t st) {
   const uint32_t tiles = blocks_for(w.n_cells, SCAN_TILE);
   k_tile_sums<<<tiles, SCAN_THREADS, 0, st>>>(w);
-  k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(w);
+  if (tiles > SCAN_PREFIX_TILES && tiles == w.n_tiles) {
+    k_tile_prefix<<<1, 1024, 0, st>>>(w);
+    k_scan_apply<true><<<tiles, SCAN_THREADS, 0, st>>>(w);
+    return 3;
+  }
+  k_scan_apply<false><<<tiles, SCAN_THREADS, 0, st>>>(w);
+  return 2;
 }
 
 #define BLOBS_DISPATCH_BOOL(v, NAME, ...) \

@@ -6,7 +6,8 @@
 namespace blobs {
 
 void launch_keys(const WorldDev& w, bool multiworld, cudaStream_t st);
-void launch_scan(const WorldDev& w, cudaStream_t st);
+// the cell scan; returns the number of kernels it launched
+uint32_t launch_scan(const WorldDev& w, cudaStream_t st);
 void launch_scatter_forces(const WorldDev& w, const float2* pos, bool multiworld, bool scatter, bool springs,
                            bool pending, cudaStream_t st);
 uint32_t launch_contacts(const WorldDev& w, const float2* pos_in, float2* pos_out, bool multiworld, bool single,

@@ -859,7 +859,7 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
         w->enqueued += 1;
       }
       mark_begin(w, PHASE_SCAN);
-      launch_scan(d, st);
+      w->enqueued += launch_scan(d, st);
       mark_end(w);
       mark_begin(w, PHASE_SCATTER);
       if (first_in_step) {
@@ -882,7 +882,7 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
       mark_end(w);
       a.contacts = 1u;
       a.do_keys = 1u;
-      w->enqueued += 4;  // two scan kernels, permute or scatter, step
+      w->enqueued += 2;  // permute or scatter, step
       w->keys_valid = true;
     } else {
       w->enqueued += 1;
@@ -916,9 +916,8 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
   }
   if (coll) {
     mark_begin(w, PHASE_SCAN);
-    launch_scan(d, st);
+    w->enqueued += launch_scan(d, st);
     mark_end(w);
-    w->enqueued += 2;
   }
   if (coll || w->has_springs) {
     mark_begin(w, PHASE_SCATTER);
