@@ -261,7 +261,7 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
   return p;
 }
 
-constexpr int STEP_THREADS = 256;
+constexpr int STEP_THREADS = 128;
 
 // Bodies with more near candidates than this take k_step_deferred.
 constexpr uint32_t DEFER_NEAR = 12;
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 // its whole warp in the O(contacts x candidates) walk or the O(near^2)
 // ordered selection.
 template <int MODE, bool HOOKS>
-__global__ void __launch_bounds__(STEP_THREADS, 4) k_step_single(WorldDev w, SingleArgs a) {
+__global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, SingleArgs a) {
   constexpr bool DEFER = !HOOKS;
   // phase 2 slots of the plain step: near candidate ids and positions,
   // thread-interleaved
@@ -824,15 +824,15 @@ void launch_scatter_cand(const WorldDev& w, const float4* a_in, float4* cand, cu
 
 void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st) {
   if (!w.n_bodies) return;
-  const uint32_t g = nblocks(w.n_bodies);
+  const uint32_t g = (w.n_bodies + STEP_THREADS - 1) / STEP_THREADS;
   if (a.rec_list || w.ev_rec) {
-    if (mode == 0) k_step_single<0, true><<<g, 256, 0, st>>>(w, a);
-    else if (mode == 1) k_step_single<1, true><<<g, 256, 0, st>>>(w, a);
-    else k_step_single<2, true><<<g, 256, 0, st>>>(w, a);
+    if (mode == 0) k_step_single<0, true><<<g, STEP_THREADS, 0, st>>>(w, a);
+    else if (mode == 1) k_step_single<1, true><<<g, STEP_THREADS, 0, st>>>(w, a);
+    else k_step_single<2, true><<<g, STEP_THREADS, 0, st>>>(w, a);
   } else {
-    if (mode == 0) k_step_single<0, false><<<g, 256, 0, st>>>(w, a);
-    else if (mode == 1) k_step_single<1, false><<<g, 256, 0, st>>>(w, a);
-    else k_step_single<2, false><<<g, 256, 0, st>>>(w, a);
+    if (mode == 0) k_step_single<0, false><<<g, STEP_THREADS, 0, st>>>(w, a);
+    else if (mode == 1) k_step_single<1, false><<<g, STEP_THREADS, 0, st>>>(w, a);
+    else k_step_single<2, false><<<g, STEP_THREADS, 0, st>>>(w, a);
   }
 }
 
