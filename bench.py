@@ -357,6 +357,8 @@ def batched_comparison(dev, steps=100, sample=1024, seed=4):
     stream = torch.cuda.current_stream(dev)
     w = native.World(scene, device=dev.index)
     w.set_stream(stream.cuda_stream)
+    # the cell edge picked by timing, as for the headline world (reloads the scene)
+    cell_scale = w.autotune(scene, dt, trial_steps=3)
     for _ in range(3):
         w.step(dt)
     w.rollout(dt, steps)  # capture
@@ -391,7 +393,7 @@ def batched_comparison(dev, steps=100, sample=1024, seed=4):
     per_body_substep = BYTES_PER_BODY_SUBSTEP + BYTES_PER_SPRING_SUBSTEP * scene.n_springs / scene.n_bodies
     achieved = per_body_substep * scene.substeps * scene.n_bodies * steps / (batched_ms / 1e3) / 1e9
     return {"worlds": scene.n_worlds, "bodies": scene.n_bodies, "springs": scene.n_springs, "steps": steps,
-            "batched_ms": batched_ms, "per_world_ms_est": per_world_ms, "speedup": per_world_ms / batched_ms,
+            "cell_scale": cell_scale, "batched_ms": batched_ms, "per_world_ms_est": per_world_ms, "speedup": per_world_ms / batched_ms,
             "batched_sphere_steps_per_s": scene.n_bodies * steps / (batched_ms / 1e3),
             "sample": "%d evenly spaced worlds (%d bodies), one rollout launch per world, scaled by body count"
                       % (len(idx), bodies),
