@@ -289,12 +289,12 @@ def run_section(args):
         torch.cuda.synchronize()
         ms += e0.elapsed_time(e1)
     contacts_last = w.contact_count()[1]
-    walk_last = w.walk_count()[1] if scene.single_collider() else None
+    deferred_last = w.deferred_count()[1] if scene.single_collider() else None
     w.close()
     print(json.dumps({"section": args.section, "bodies": scene.n_bodies, "colliders": scene.n_colliders,
                       "worlds": scene.n_worlds, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": ms / args.steps, "contacts_last_substep": contacts_last,
-                      "deferred_bodies_last_substep": walk_last,
+                      "deferred_bodies_last_substep": deferred_last,
                       "phase_us_per_substep": {k: 1e3 * v / args.steps / scene.substeps for k, v in phase.items()}}),
           flush=True)
 
@@ -506,6 +506,55 @@ def sparse_comparison(dev, seed=1):
             "speedup": cpu_s * 1e3 / gpu_ms, "final_state_bit_exact": exact}
 
 
+def events_comparison(dev, settle=200, steps=5, seed=2):
+    """The headline world with the CollisionEvent stream on (physics.rs:304-311:
+    one event per contact per substep): `settle` steps from t = 0 without
+    events, then `steps` steps with them -- each step between its own
+    CUDA-event pair (L2 flushed before it), its events drained to the host
+    and put in the reference's order after it (host time, outside the
+    events) -- against the same steps with the stream off."""
+    import numpy as np
+    import torch
+    from blobs_gb300 import native, scenes
+    scene = scenes.dense_spheres(seed=seed)
+    stream = torch.cuda.current_stream(dev)
+    w = native.World(scene, device=dev.index)
+    w.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    out = {}
+    for on in (False, True):
+        w.load(scene)
+        for _ in range(settle):
+            w.step(scene.dt)
+        if on:
+            w.set_events(True, capacity=12_000_000)
+        ms, drain_s, n_events = [], [], 0
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            w.step(scene.dt)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            if on:
+                t0 = time.perf_counter()
+                n_events += len(w.drain_events()[0])
+                drain_s.append(time.perf_counter() - t0)
+        if on:
+            w.set_events(False)
+            out["events_on"] = {"ms_per_step": float(np.mean(ms)), "events_per_step": n_events / steps,
+                                "drain_ms_per_step": 1e3 * float(np.mean(drain_s))}
+        else:
+            out["events_off"] = {"ms_per_step": float(np.mean(ms))}
+    w.close()
+    out.update({"bodies": scene.n_bodies, "steps": "%d-%d of the rollout" % (settle, settle + steps - 1),
+                "note": "device time per step with the stream on (the contact kernels append one 32-byte record "
+                        "per contact) and off; the drain copies the step's events to the host and sorts them "
+                        "into the reference's order"})
+    return out
+
+
 def adjoint_comparison(dev, steps=120, every=16, seed=5, finite_steps=32):
     """256 worlds x 2,048 spheres with 1,024 springs each: a 120-step forward
     pass (one CUDA-graph rollout) against the same rollout recorded with a
@@ -644,7 +693,7 @@ def run_ours(args):
         if i in timed_set:
             launches += world.kernel_launches() - k0
         if i + 1 in readouts:  # synchronising reads, outside the events
-            counts[i + 1] = (world.contact_count()[1], world.walk_count()[1])
+            counts[i + 1] = (world.contact_count()[1], world.deferred_count()[1])
     barrier()
     clk = clocks.stop()
     ms = np.array([s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)])
@@ -722,7 +771,7 @@ def run_ours(args):
                     "ms_per_step_first_100": float(ms[:100].mean()), "ms_per_step_last_100": float(ms[-100:].mean()),
                     "max_step_ms": float(ms.max()),
                     "contacts_per_substep_after": {str(k): v[0] for k, v in counts.items()},
-                    "walk_bodies_per_substep_after": {str(k): v[1] for k, v in counts.items()},
+                    "deferred_bodies_per_substep_after": {str(k): v[1] for k, v in counts.items()},
                     "note": "every step of the configuration's 1,000-step rollout from t=0, each between its own "
                             "CUDA-event pair, L2 flushed before each (outside the events); the counts are of the "
                             "last substep after 1, 200, 500 and 1,000 steps"},
@@ -748,6 +797,8 @@ def run_ours(args):
         line["batched"] = batched_comparison(dev)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_comparison(dev)
+    if rank == 0 and not args.no_events:
+        line["events"] = events_comparison(dev)
     if rank == 0 and not args.no_general:
         line["general"] = general_comparison(dev)
     if rank == 0 and not args.no_literal:
@@ -772,6 +823,7 @@ def main():
     ap.add_argument("--no-general", action="store_true")
     ap.add_argument("--no-literal", action="store_true", help="skip the 2000 x 2000 literal-box run")
     ap.add_argument("--no-sparse", action="store_true", help="skip the 1,000-sphere full-run comparison")
+    ap.add_argument("--no-events", action="store_true", help="skip the collision-event stream comparison")
     ap.add_argument("--section", choices=["general", "batched", "dense"], default=None,
                     help="run one secondary workload alone (profiling driver), print its phase times; dense: the "
                          "1M-sphere world at 80%% packing, the density of the rollout's settled pile")

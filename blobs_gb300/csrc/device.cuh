@@ -147,8 +147,8 @@ struct WorldDev {
   unsigned long long* contacts_total;
   unsigned long long* pushouts_total;
   uint32_t* contacts_sub;    // contacts of the most recent substep
-  unsigned long long* walk_total;  // bodies whose contacts took the exact selection walk (many candidates)
-  uint32_t* walk_sub;        // the same in the most recent substep
+  unsigned long long* defer_total;  // bodies deferred to a warp each (many candidates or near candidates)
+  uint32_t* defer_sub;       // the same in the most recent substep
   uint32_t* status;
 };
 

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(WorldDev w) {
   if (threadIdx.x == 0) w.tile_sums[blockIdx.x] = t;
   if (blockIdx.x == 0 && threadIdx.x < COUNTER_BINS) {
     if (w.contacts_sub) w.contacts_sub[threadIdx.x] = 0u;
-    if (w.walk_sub) w.walk_sub[threadIdx.x] = 0u;
+    if (w.defer_sub) w.defer_sub[threadIdx.x] = 0u;
     if (threadIdx.x == 0 && w.defer_count) *w.defer_count = 0u;
   }
 }

@@ -163,14 +163,14 @@ __device__ __forceinline__ void single_event(const WorldDev& w, const SingleArgs
   record_event(w, c, lo, a.v_in[j], a.v_in[jl]);
 }
 
-__device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush, bool walked) {
+__device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts, uint32_t npush, bool deferred) {
   uint32_t t = ncontacts, p = npush;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     t += __shfl_xor_sync(0xffffffffu, t, o);
     p += __shfl_xor_sync(0xffffffffu, p, o);
   }
-  const uint32_t nw = __popc(__ballot_sync(0xffffffffu, walked));
+  const uint32_t nw = __popc(__ballot_sync(0xffffffffu, deferred));
   if ((threadIdx.x & 31u) == 0u) {
     const uint32_t bin = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (COUNTER_BINS - 1);
     if (t) {
@@ -179,8 +179,8 @@ __device__ __forceinline__ void count_warp(const WorldDev& w, uint32_t ncontacts
     }
     if (p) atomicAdd(w.pushouts_total + bin, (unsigned long long)p);
     if (nw) {
-      atomicAdd(w.walk_total + bin, (unsigned long long)nw);
-      atomicAdd(w.walk_sub + bin, nw);
+      atomicAdd(w.defer_total + bin, (unsigned long long)nw);
+      atomicAdd(w.defer_sub + bin, nw);
     }
   }
 }
@@ -485,21 +485,18 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 }
 
 // HOOKS: compiled with the adjoint's contact recording and the collision
-// event stream.  The plain step (no hooks) leaves a body whose 3x3 cells
-// hold too many candidates for its near mask, or which has more than
-// DEFER_NEAR near candidates, to k_step_deferred: one such body would hold
-// its whole warp in the O(contacts x candidates) walk or the O(near^2)
-// ordered selection.
+// event stream.  A body whose 3x3 cells hold too many candidates for its
+// near mask, or which has more than DEFER_NEAR near candidates, is left to
+// k_step_deferred: one such body would hold its whole warp in the
+// O(contacts x candidates) walk or the O(near^2) ordered selection.
 template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, SingleArgs a) {
-  constexpr bool DEFER = !HOOKS;
   // phase 2 slots of the plain step: near candidate ids and positions,
   // thread-interleaved
-  __shared__ uint32_t s_ids[DEFER ? DEFER_NEAR * STEP_THREADS : 1], s_qs[DEFER ? DEFER_NEAR * STEP_THREADS : 1];
+  __shared__ uint32_t s_ids[!HOOKS ? DEFER_NEAR * STEP_THREADS : 1], s_qs[!HOOKS ? DEFER_NEAR * STEP_THREADS : 1];
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t ncontacts = 0, npush = 0;
-  bool walked = false;
   bool deferred = false;  // contacts (and the rest of the body's substep) left to k_step_deferred
   if (j < w.n_bodies) {
     const float4 av = a.a_in[j];
@@ -545,15 +542,12 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
         const uint32_t t2 = t;
         near_range(C, s, r, c, s2, s2 + l2, t, nb);
         // Phase 2: the near candidates in ascending arena id
-        if (DEFER && __popcll(nb) > DEFER_NEAR) deferred = true;
-        else if (DEFER) p = apply_near_s<MODE>(w, a, nb, s0, s1, s2, t1, t2, c, p0, s, r, k.m, ncontacts, npush,
-                                                 s_ids + threadIdx.x, s_qs + threadIdx.x);
+        if (__popcll(nb) > DEFER_NEAR) deferred = true;
+        else if (!HOOKS) p = apply_near_s<MODE>(w, a, nb, s0, s1, s2, t1, t2, c, p0, s, r, k.m, ncontacts, npush,
+                                                  s_ids + threadIdx.x, s_qs + threadIdx.x);
         else p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
-      } else if (DEFER) {
-        deferred = true;
       } else {
-        p = contacts_walk<MODE, HOOKS>(w, a, segments(w, wp, own_key), j, c, p0, s, r, k.m, ncontacts, npush, nrec);
-        walked = true;
+        deferred = true;
       }
     } else if (a.contacts) {
       // cells on the grid edge (the torus wraps): general segments
@@ -603,21 +597,18 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
             if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
           }
         }
-      } else if (DEFER) {
-        deferred = true;
       } else {
-        p = contacts_walk<MODE, HOOKS>(w, a, g, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
-        walked = true;
+        deferred = true;
       }
     }
 
-    if (HOOKS && a.rec_list) {
+    if (HOOKS && a.rec_list && !deferred) {
       a.rec_n[c] = nrec;
       if (nrec) atomicMax(a.rec_max, nrec);
     }
     if (!deferred) finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
   }
-  if (DEFER && a.contacts) {
+  if (a.contacts) {
     // append the deferred bodies to the list k_step_deferred works through
     const uint32_t dm = __ballot_sync(0xffffffffu, deferred);
     if (dm) {
@@ -631,7 +622,7 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
       }
     }
   }
-  if (a.contacts) count_warp(w, ncontacts, npush, walked || deferred);
+  if (a.contacts) count_warp(w, ncontacts, npush, deferred);
 }
 
 // The bodies k_step_single deferred (many candidates or many near
@@ -642,7 +633,7 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
 // one lane applies them in that order -- the reference's pair order for this
 // body -- then finishes the body's substep.  More than DEFER_CAP contacts:
 // the exact selection walk on one lane.
-template <int MODE>
+template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, SingleArgs a) {
   __shared__ DeferWarp dsm[DEFER_THREADS / 32];
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
@@ -705,6 +696,7 @@ __global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, Sin
       __syncwarp();
       if (lane == 0) {
         float2 p = p0;
+        uint32_t nrec = 0;
         for (uint32_t i = 0; i < cnt; ++i) {
           const uint32_t e = S.order[i];
           if (e >= cnt) {  // ranks are a permutation when the partner ids are distinct
@@ -716,18 +708,28 @@ __global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, Sin
           const bool pushed = __float_as_uint(cr.z) != 0u;
           if (pushed) p = add(p, c > c2 ? v2(0.01f, 0.0f) : v2(-0.01f, -0.0f));
           p = add(p, v2(cr.x, cr.y));
+          if (HOOKS && a.rec_list) record_contact(w, a, c, c2, pushed, nrec);
           if (c2 < c) {
             ++tc;
             tp += pushed ? 1u : 0u;
+            if (HOOKS && w.ev_rec) single_event(w, a, c, j, c2);
           }
+        }
+        if (HOOKS && a.rec_list) {
+          a.rec_n[c] = nrec;
+          if (nrec) atomicMax(a.rec_max, nrec);
         }
         finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
       }
     } else if (lane == 0) {
       uint32_t nc = 0, np = 0, nr = 0;
-      const float2 p = contacts_walk<MODE, false>(w, a, g, j, c, p0, s, r, k.m, nc, np, nr);
+      const float2 p = contacts_walk<MODE, HOOKS>(w, a, g, j, c, p0, s, r, k.m, nc, np, nr);
       tc += nc;
       tp += np;
+      if (HOOKS && a.rec_list) {
+        a.rec_n[c] = nr;
+        if (nr) atomicMax(a.rec_max, nr);
+      }
       finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
     }
     __syncwarp();
@@ -838,9 +840,15 @@ void launch_step_single(const WorldDev& w, const SingleArgs& a, int mode, cudaSt
 
 void launch_step_deferred(const WorldDev& w, const SingleArgs& a, int mode, cudaStream_t st) {
   if (!w.n_bodies || !w.defer_list) return;
-  if (mode == 0) k_step_deferred<0><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
-  else if (mode == 1) k_step_deferred<1><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
-  else k_step_deferred<2><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+  if (a.rec_list || w.ev_rec) {
+    if (mode == 0) k_step_deferred<0, true><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+    else if (mode == 1) k_step_deferred<1, true><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+    else k_step_deferred<2, true><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+  } else {
+    if (mode == 0) k_step_deferred<0, false><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+    else if (mode == 1) k_step_deferred<1, false><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+    else k_step_deferred<2, false><<<DEFER_BLOCKS, DEFER_THREADS, 0, st>>>(w, a);
+  }
 }
 
 void launch_keys_single(const WorldDev& w, const float4* A, int mode, cudaStream_t st) {

@@ -152,7 +152,7 @@ void scan_counts(uint32_t* count, uint32_t* start, uint32_t n, uint32_t* tile_su
   d.n_tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   d.tile_sums = tile_sums;
   d.contacts_sub = sub_bins;
-  d.walk_sub = sub_bins;
+  d.defer_sub = sub_bins;
   launch_scan(d, st);
 }
 

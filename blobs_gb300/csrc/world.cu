@@ -26,8 +26,8 @@ struct Counters {
   unsigned long long contacts_total[COUNTER_BINS];
   unsigned long long pushouts_total[COUNTER_BINS];
   uint32_t contacts_sub[COUNTER_BINS];
-  unsigned long long walk_total[COUNTER_BINS];
-  uint32_t walk_sub[COUNTER_BINS];
+  unsigned long long defer_total[COUNTER_BINS];
+  uint32_t defer_sub[COUNTER_BINS];
   uint32_t status;
   uint32_t pad[3];
   unsigned long long contacts() const {
@@ -35,14 +35,14 @@ struct Counters {
     for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += contacts_total[i];
     return t;
   }
-  unsigned long long walks() const {
+  unsigned long long deferred() const {
     unsigned long long t = 0;
-    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += walk_total[i];
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += defer_total[i];
     return t;
   }
-  unsigned long long walks_sub() const {
+  unsigned long long deferred_sub() const {
     unsigned long long t = 0;
-    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += walk_sub[i];
+    for (uint32_t i = 0; i < COUNTER_BINS; ++i) t += defer_sub[i];
     return t;
   }
   unsigned long long pushouts() const {
@@ -896,8 +896,8 @@ void enqueue_substep(blobs_world* w, float dt, float old_dt, bool pending, bool 
     a.v_out = d.sv[w->v_tracks() ? out : w->vbuf];
     mark_begin(w, coll ? PHASE_CONTACT : PHASE_INTEGRATE);
     launch_step_single(d, a, w->single_mode, st);
-    if (coll && !(a.rec_list || d.ev_rec)) {
-      // the plain step defers bodies with many candidates to a warp each
+    if (coll) {
+      // bodies with many candidates, deferred by the step kernel, a warp each
       launch_step_deferred(d, a, w->single_mode, st);
       w->enqueued += 1;
     }
@@ -1240,8 +1240,8 @@ int blobs_world_load(blobs_world* w, const blobs_scene* scene, float old_dt) {
   d.contacts_total = counters->contacts_total;
   d.pushouts_total = counters->pushouts_total;
   d.contacts_sub = counters->contacts_sub;
-  d.walk_total = counters->walk_total;
-  d.walk_sub = counters->walk_sub;
+  d.defer_total = counters->defer_total;
+  d.defer_sub = counters->defer_sub;
   d.status = &counters->status;
   w->dcounters = counters;
 
@@ -1461,13 +1461,13 @@ int blobs_world_pushout_count(blobs_world* w, uint64_t* total) {
   return st;
 }
 
-int blobs_world_walk_count(blobs_world* w, uint64_t* total, uint64_t* last_substep) {
+int blobs_world_deferred_count(blobs_world* w, uint64_t* total, uint64_t* last_substep) {
   if (!w) return BLOBS_ERR_INVALID_HANDLE;
   if (!w->loaded) return BLOBS_ERR_STATE;
   cudaSetDevice(w->cfg.device);
   int st = read_status(w);
-  if (total) *total = w->hcounters->walks();
-  if (last_substep) *last_substep = w->hcounters->walks_sub();
+  if (total) *total = w->hcounters->deferred();
+  if (last_substep) *last_substep = w->hcounters->deferred_sub();
   return st;
 }
 

@@ -92,7 +92,7 @@ def lib() -> ctypes.CDLL:
         "blobs_world_read_snapshots": (i32, [_P, _P]),
         "blobs_world_contact_count": (i32, [_P, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "blobs_world_pushout_count": (i32, [_P, ctypes.POINTER(u64)]),
-        "blobs_world_walk_count": (i32, [_P, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
+        "blobs_world_deferred_count": (i32, [_P, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "blobs_world_time": (i32, [_P, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "blobs_world_joint_order": (i32, [_P, _P, ctypes.POINTER(u32)]),
         "blobs_world_snapshot": (i32, [_P]),
@@ -428,10 +428,10 @@ class World:
         check(lib().blobs_world_contact_count(self._h, ctypes.byref(t), ctypes.byref(l)), "contact_count")
         return int(t.value), int(l.value)
 
-    def walk_count(self):
-        """(total, last substep) bodies whose contacts took the selection walk."""
+    def deferred_count(self):
+        """(total, last substep) bodies whose contacts were resolved by a warp each."""
         t, l = ctypes.c_uint64(), ctypes.c_uint64()
-        check(lib().blobs_world_walk_count(self._h, ctypes.byref(t), ctypes.byref(l)), "walk_count")
+        check(lib().blobs_world_deferred_count(self._h, ctypes.byref(t), ctypes.byref(l)), "deferred_count")
         return int(t.value), int(l.value)
 
     def pushout_count(self) -> int:

@@ -226,10 +226,10 @@ int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_su
  * (physics.rs:272-286) since load. */
 int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
 /* No counterpart in the reference (a cost diagnostic): bodies of the
- * single-sphere path whose 3x3 cells held too many candidates for the
- * bit-mask pass, so their contacts took the exact selection walk -- since
- * load and in the last substep. */
-int blobs_world_walk_count(blobs_world* w, uint64_t* total, uint64_t* last_substep);
+ * single-sphere path whose 3x3 cells held more than 64 candidates, or which
+ * had more than 12 near candidates, and whose contacts were therefore
+ * resolved by a warp of their own -- since load and in the last substep. */
+int blobs_world_deferred_count(blobs_world* w, uint64_t* total, uint64_t* last_substep);
 /* The broadphase output for the current collider snapshots: every collider
  * pair (hi, lo), hi > lo in arena order, whose cells are 3x3 neighbours in
  * its world's grid (contacts_only = 0), or only the pairs the contact pass
