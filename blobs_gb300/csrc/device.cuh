@@ -289,8 +289,16 @@ struct SingleArgs {
 // Append one collision event (physics.rs:304-311): the pair (a, b) with
 // a > b in collider order and the parents' calculated_velocity at the start
 // of the contact pass.
+// The lanes of a warp that append together take their slots with one atomic
+// (the buffer is put in order on the host, so any order of slots will do).
 __device__ __forceinline__ void record_event(const WorldDev& w, uint32_t a, uint32_t b, float2 va, float2 vb) {
-  const uint32_t k = atomicAdd(w.ev_count, 1u);
+  const uint32_t active = __activemask();
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t leader = (uint32_t)(__ffs(active) - 1);
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(w.ev_count, (uint32_t)__popc(active));
+  base = __shfl_sync(active, base, leader);
+  const uint32_t k = base + (uint32_t)__popc(active & ((1u << lane) - 1u));
   if (k < w.ev_cap) {
     w.ev_rec[k] = make_uint4(*w.ev_seq, a, b, 0u);
     w.ev_vel[k] = make_float4(va.x, va.y, vb.x, vb.y);
