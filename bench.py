@@ -509,7 +509,8 @@ def sparse_comparison(dev, seed=1):
 def events_comparison(dev, settle=200, steps=5, seed=2):
     """The headline world with the CollisionEvent stream on (physics.rs:304-311:
     one event per contact per substep): `settle` steps from t = 0 without
-    events, then `steps` steps with them -- each step between its own
+    events, one untimed step with them (the step graphs are captured again),
+    then `steps` steps with them -- each step between its own
     CUDA-event pair (L2 flushed before it), its events drained to the host
     and put in the reference's order after it (host time, outside the
     events) -- against the same steps with the stream off."""
@@ -528,6 +529,10 @@ def events_comparison(dev, settle=200, steps=5, seed=2):
             w.step(scene.dt)
         if on:
             w.set_events(True, capacity=12_000_000)
+            w.step(scene.dt)  # the step graphs are captured again with the stream on (untimed)
+            w.drain_events()
+        else:
+            w.step(scene.dt)
         ms, drain_s, n_events = [], [], 0
         for _ in range(steps):
             flush.zero_()
@@ -548,7 +553,7 @@ def events_comparison(dev, settle=200, steps=5, seed=2):
         else:
             out["events_off"] = {"ms_per_step": float(np.mean(ms))}
     w.close()
-    out.update({"bodies": scene.n_bodies, "steps": "%d-%d of the rollout" % (settle, settle + steps - 1),
+    out.update({"bodies": scene.n_bodies, "steps": "%d-%d of the rollout" % (settle + 1, settle + steps),
                 "note": "device time per step with the stream on (the contact kernels append one 32-byte record "
                         "per contact) and off; the drain copies the step's events to the host and sorts them "
                         "into the reference's order"})
