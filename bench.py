@@ -402,12 +402,27 @@ def batched_comparison(dev, steps=100, sample=1024, seed=4):
             "cpu_baseline": cpu_batched(scene)}
 
 
-def general_comparison(dev, steps=10, warmup=3, seed=3):
-    """The general path: 200,000 bodies with 1-4 sphere
-    colliders each, 50,000 fixed joints (coloured Gauss-Seidel, 4
-    iterations), 100,000 damped springs, box 1500 x 1500, dt = 1/120.
-    Device time of `steps` single steps after `warmup`, L2 flushed before
-    each, on the world's stream."""
+def _rollout_ms(w, scene, stream, flush):
+    """Every step of the scene's rollout from its loaded state, each between
+    its own CUDA-event pair, L2 flushed before each (outside the events)."""
+    import numpy as np
+    import torch
+    n = scene.n_steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    for e0, e1 in ev:
+        flush.zero_()
+        e0.record(stream)
+        w.step(scene.dt)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return np.array([e0.elapsed_time(e1) for e0, e1 in ev])
+
+
+def general_comparison(dev, seed=3):
+    """The general path: 200,000 bodies with 1-4 sphere colliders each,
+    50,000 fixed joints (4 iterations), 100,000 damped springs, box
+    1500 x 1500, dt = 1/120: device time of every step of its 500-step
+    rollout from t = 0, on the world's stream."""
     import torch
     from blobs_gb300 import native, scenes
     scene = scenes.jointed_bodies(seed=seed)
@@ -415,32 +430,21 @@ def general_comparison(dev, steps=10, warmup=3, seed=3):
     w = native.World(scene, device=dev.index)
     w.set_stream(stream.cuda_stream)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-    for _ in range(warmup):
-        w.step(scene.dt)
-    torch.cuda.synchronize()
     k0 = w.kernel_launches()
-    ms = 0.0
-    for _ in range(steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        w.step(scene.dt)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms += e0.elapsed_time(e1)
-    launches = (w.kernel_launches() - k0) / steps
+    ms = _rollout_ms(w, scene, stream, flush)
+    launches = (w.kernel_launches() - k0) / scene.n_steps
     w.close()
     return {"bodies": scene.n_bodies, "colliders": scene.n_colliders, "joints": scene.n_joints,
-            "springs": scene.n_springs, "steps": steps, "ms_per_step": ms / steps,
-            "body_steps_per_s": scene.n_bodies * steps / (ms / 1e3), "kernel_launches_per_step": launches,
-            "cpu_baseline": cpu_general()}
+            "springs": scene.n_springs, "steps": scene.n_steps, "ms_per_step": float(ms.mean()),
+            "ms_per_step_first_100": float(ms[:100].mean()), "ms_per_step_last_100": float(ms[-100:].mean()),
+            "body_steps_per_s": scene.n_bodies * scene.n_steps / (ms.sum() / 1e3),
+            "kernel_launches_per_step": launches, "cpu_baseline": cpu_general()}
 
 
-def literal_box_comparison(dev, steps=20, warmup=3, seed=2):
+def literal_box_comparison(dev, seed=2):
     """The 1,000,000-sphere workload in the literal 2000 x 2000 walled box
-    (0.85% packing instead of 40%): device time of `steps` single steps after
-    `warmup`, L2 flushed before each, on the world's stream, at the
-    autotuned cell edge."""
+    (0.85% packing instead of 40%) at the autotuned cell edge: device time of
+    every step of its 1,000-step rollout from t = 0."""
     import torch
     from blobs_gb300 import native, scenes
     scene = scenes.dense_spheres(seed=seed, n=1_000_000, literal_box=True)
@@ -449,22 +453,13 @@ def literal_box_comparison(dev, steps=20, warmup=3, seed=2):
     w.set_stream(stream.cuda_stream)
     cell_scale = w.autotune(scene, scene.dt, trial_steps=3)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-    for _ in range(warmup):
-        w.step(scene.dt)
-    torch.cuda.synchronize()
-    ms = 0.0
-    for _ in range(steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        w.step(scene.dt)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms += e0.elapsed_time(e1)
+    ms = _rollout_ms(w, scene, stream, flush)
     contacts_total, contacts_last = w.contact_count()
     w.close()
-    return {"bodies": scene.n_bodies, "box": float(scene.world_box[0, 2] - scene.world_box[0, 0]), "steps": steps,
-            "ms_per_step": ms / steps, "sphere_steps_per_s": scene.n_bodies * steps / (ms / 1e3),
+    return {"bodies": scene.n_bodies, "box": float(scene.world_box[0, 2] - scene.world_box[0, 0]),
+            "steps": scene.n_steps, "ms_per_step": float(ms.mean()), "ms_per_step_first_100": float(ms[:100].mean()),
+            "ms_per_step_last_100": float(ms[-100:].mean()),
+            "sphere_steps_per_s": scene.n_bodies * scene.n_steps / (ms.sum() / 1e3),
             "contacts_last_substep": contacts_last, "cell_scale": cell_scale}
 
 
