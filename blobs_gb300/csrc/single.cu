@@ -275,49 +275,6 @@ struct DeferWarp {
   uint32_t order[DEFER_CAP];           // contacts in ascending partner id
 };
 
-// Phase 2: the near candidates of body c in ascending arena id (the
-// reference's pair order for this body, physics.rs:244-249), the warp's
-// lanes in step.  Bit t of `near` is candidate t of the rows starting at
-// cell-order positions s0, s1, s2 and at bits 0, t1, t2.
-template <int MODE, bool HOOKS>
-__device__ __forceinline__ float2 apply_near(const WorldDev& w, const SingleArgs& a, unsigned long long near,
-                                             uint32_t s0, uint32_t s1, uint32_t s2, uint32_t t1, uint32_t t2,
-                                             uint32_t j, uint32_t c, float2 p0, float2 s, float r, float m,
-                                             uint32_t& ncontacts, uint32_t& npush, uint32_t& nrec) {
-  const float4* __restrict__ C = a.cand;
-  float2 p = p0;
-  while (near) {
-    unsigned long long best_bit = 0ull;
-    uint32_t best = 0xffffffffu;
-    float4 bo = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (unsigned long long mk = near; mk; mk &= mk - 1ull) {
-      const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
-      const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
-      const float4 o = C[q];
-      const uint32_t c2 = __float_as_uint(o.w);
-      if (c2 < best) {
-        best = c2;
-        bo = o;
-        best_bit = mk & (~mk + 1ull);
-      }
-      if ((near & (near - 1ull)) == 0ull) break;  // one near candidate needs no ordering
-    }
-    near &= ~best_bit;
-    if (best >= w.n_bodies || best == c) continue;
-    const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[best].x;
-    SinglePair sp;
-    if (!single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
-    if (sp.pushed) p = add(p, sp.push);
-    p = add(p, sp.corr);
-    if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
-    if (best < c) {
-      ++ncontacts;
-      npush += sp.pushed ? 1u : 0u;
-      if (HOOKS && w.ev_rec) single_event(w, a, c, j, best);
-    }
-  }
-  return p;
-}
 
 }  // namespace
 
@@ -411,11 +368,12 @@ __device__ __forceinline__ void finish_single(const WorldDev& w, const SingleArg
 // candidates' ids are gathered into this thread's shared-memory slots first
 // (independent loads), then the ascending-id selection runs over shared
 // memory and only the chosen candidate's record is loaded again.
-template <int MODE>
+template <int MODE, bool HOOKS>
 __device__ __forceinline__ float2 apply_near_s(const WorldDev& w, const SingleArgs& a, unsigned long long near,
                                                uint32_t s0, uint32_t s1, uint32_t s2, uint32_t t1, uint32_t t2,
-                                               uint32_t c, float2 p0, float2 s, float r, float m,
-                                               uint32_t& ncontacts, uint32_t& npush, uint32_t* ids, uint32_t* qs) {
+                                               uint32_t j, uint32_t c, float2 p0, float2 s, float r, float m,
+                                               uint32_t& ncontacts, uint32_t& npush, uint32_t& nrec, uint32_t* ids,
+                                               uint32_t* qs, uint32_t* ev_lo, uint32_t& nev) {
   const float4* __restrict__ C = a.cand;
   const uint32_t* __restrict__ Cw = reinterpret_cast<const uint32_t*>(a.cand);
   float2 p = p0;
@@ -444,9 +402,11 @@ __device__ __forceinline__ float2 apply_near_s(const WorldDev& w, const SingleAr
     if (!single_pair(w, a, c, p0, s, r, m, best, v2(bo.x, bo.y), bo.z, m2, sp)) continue;
     if (sp.pushed) p = add(p, sp.push);
     p = add(p, sp.corr);
+    if (HOOKS && a.rec_list) record_contact(w, a, c, best, sp.pushed, nrec);
     if (best < c) {
       ++ncontacts;
       npush += sp.pushed ? 1u : 0u;
+      if (HOOKS && w.ev_rec) ev_lo[(nev++) * STEP_THREADS] = best;  // appended by the warp afterwards
     }
   }
   return p;
@@ -493,7 +453,11 @@ template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, SingleArgs a) {
   // phase 2 slots of the plain step: near candidate ids and positions,
   // thread-interleaved
-  __shared__ uint32_t s_ids[!HOOKS ? DEFER_NEAR * STEP_THREADS : 1], s_qs[!HOOKS ? DEFER_NEAR * STEP_THREADS : 1];
+  __shared__ uint32_t s_ids[DEFER_NEAR * STEP_THREADS], s_qs[DEFER_NEAR * STEP_THREADS];
+  // event stream: the partners of this thread's events of phase 2, appended
+  // together by the warp after it
+  __shared__ uint32_t s_ev[HOOKS ? DEFER_NEAR * STEP_THREADS : 1];
+  uint32_t nev = 0;
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t ncontacts = 0, npush = 0;
@@ -543,9 +507,9 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
         near_range(C, s, r, c, s2, s2 + l2, t, nb);
         // Phase 2: the near candidates in ascending arena id
         if (__popcll(nb) > DEFER_NEAR) deferred = true;
-        else if (!HOOKS) p = apply_near_s<MODE>(w, a, nb, s0, s1, s2, t1, t2, c, p0, s, r, k.m, ncontacts, npush,
-                                                  s_ids + threadIdx.x, s_qs + threadIdx.x);
-        else p = apply_near<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec);
+        else p = apply_near_s<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec,
+                                           s_ids + threadIdx.x, s_qs + threadIdx.x, s_ev + (HOOKS ? threadIdx.x : 0u),
+                                           nev);
       } else {
         deferred = true;
       }
@@ -607,6 +571,40 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
       if (nrec) atomicMax(a.rec_max, nrec);
     }
     if (!deferred) finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
+  }
+  if (HOOKS && w.ev_rec) {
+    // phase 2's events of the warp: one atomic for all of them
+    uint32_t incl = nev;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (total) {
+      if (lane == 0) base = atomicAdd(w.ev_count, total);
+      base = __shfl_sync(0xffffffffu, base, 0);
+    }
+    if (nev) {
+      const uint32_t seq = *w.ev_seq;
+      const uint32_t c = __float_as_uint(a.a_in[j].w);
+      const float2 va = a.v_in[j];
+      for (uint32_t i = 0; i < nev; ++i) {
+        const uint32_t slot = base + (incl - nev) + i;
+        const uint32_t lo = s_ev[i * STEP_THREADS + threadIdx.x];
+        const uint32_t jl = w.where[lo];
+        if (jl >= w.n_bodies) {
+          atomicOr(w.status, ST_BAD_INDEX);
+          continue;
+        }
+        if (slot < w.ev_cap) {
+          const float2 vb = a.v_in[jl];
+          w.ev_rec[slot] = make_uint4(seq, c, lo, 0u);
+          w.ev_vel[slot] = make_float4(va.x, va.y, vb.x, vb.y);
+        }
+      }
+    }
   }
   if (a.contacts) {
     // append the deferred bodies to the list k_step_deferred works through
