@@ -107,10 +107,12 @@ struct SinglePair {
 // The increment to body c's position from its contact with body c2, in the
 // reference's terms (a = the higher arena index).  Returns false if the pair
 // is not in contact.  The push-out branch (physics.rs:272-286) uses the
-// positions at the start of the contact pass.
+// positions at the start of the contact pass: p, or with LOAD_P the one
+// loaded from body c's slot jc.
+template <bool LOAD_P = false>
 __device__ __forceinline__ bool single_pair(const WorldDev& w, const SingleArgs& a, uint32_t c, float2 p, float2 s,
                                             float r, float m, uint32_t c2, float2 s2, float r2, float m2,
-                                            SinglePair& out) {
+                                            SinglePair& out, uint32_t jc = 0u) {
   const float dx = s.x - s2.x, dy = s.y - s2.y;
   const float mind = r + r2;
   float d = sqrtf((dx * dx) + (dy * dy));
@@ -120,6 +122,10 @@ __device__ __forceinline__ bool single_pair(const WorldDev& w, const SingleArgs&
   out.pushed = false;
   out.push = v2(0.0f, 0.0f);
   if (d < 1e-6f) {
+    if (LOAD_P) {
+      const float4 b1 = a.b_in[jc];
+      p = v2(b1.x, b1.y);
+    }
     const float4 b2 = a.b_in[w.where[c2]];
     const float2 p2 = v2(b2.x, b2.y);
     const float2 pa = add(hi ? p : p2, v2(0.01f, 0.0f));
@@ -263,8 +269,11 @@ __device__ float2 contacts_walk(const WorldDev& w, const SingleArgs& a, const Se
 
 constexpr int STEP_THREADS = 128;
 
-// Bodies with more near candidates than this take k_step_deferred.
+// Bodies with more near candidates than this take k_step_deferred (the
+// per-lane ordered selection is O(near^2)); with phase 2 shared out over
+// the warp, more than WARP_NEAR.
 constexpr uint32_t DEFER_NEAR = 12;
+constexpr uint32_t WARP_NEAR = 32;
 constexpr uint32_t DEFER_CAP = 256;    // contacts a deferred body's warp ranks in shared memory
 constexpr int DEFER_THREADS = 128;
 constexpr uint32_t DEFER_BLOCKS = 152 * 8;
@@ -412,6 +421,120 @@ __device__ __forceinline__ float2 apply_near_s(const WorldDev& w, const SingleAr
   return p;
 }
 
+// Phase 2 of the plain step in a uniform world, shared out over the warp's
+// lanes.  The near candidates of each lane get consecutive slots of the
+// warp's PairSlots (the lane's range, in lane order); every lane computes
+// the corrections of slots lane, lane + 32, ... with the owner's snapshot,
+// radius, mass and id taken by shuffle, and stores each at its rank by
+// partner id within the owner's range; then each owner adds its
+// corrections in that order, the reference's pair order for this body.
+// The exact tests and corrections (a square root and three divisions each)
+// thus run on all lanes however unevenly the near candidates fall.  A warp
+// with more than PAIR_CAP slots works in rounds of whole ranges.
+constexpr uint32_t PAIR_CAP = 128;
+
+struct PairSlots {
+  uint32_t id[PAIR_CAP];  // partner arena id
+  uint32_t q[PAIR_CAP];   // partner's position in the candidate array
+  float cx[PAIR_CAP];     // correction, at its rank in the owner's range
+  float cy[PAIR_CAP];
+  uint8_t fl[PAIR_CAP];   // at the rank: 1 contact, 2 pushed out, 4 partner id below the owner's
+  uint8_t own[PAIR_CAP];  // owner lane
+};
+
+// Correction of slot e for its owner (whose values the caller shuffled in),
+// stored at the slot's rank in the owner's range [o0, o0 + okk).
+template <int MODE>
+__device__ __forceinline__ void shared_pair(const WorldDev& w, const SingleArgs& a, PairSlots& S, uint32_t e,
+                                            uint32_t jown, float2 so, float ro, float mo, uint32_t co, uint32_t o0,
+                                            uint32_t okk) {
+  const uint32_t id = S.id[e];
+  // rank in the owner's range (ties, which distinct bodies never make,
+  // broken by slot so that the ranks stay a permutation)
+  uint32_t rank = 0;
+  for (uint32_t i = 0; i < okk; ++i) {
+    const uint32_t idi = S.id[o0 + i];
+    rank += (idi < id || (idi == id && o0 + i < e)) ? 1u : 0u;
+  }
+  uint32_t f = 0u;
+  SinglePair sp;
+  sp.corr = v2(0.0f, 0.0f);
+  if (id < w.n_bodies && id != co) {
+    const float4 bo = a.cand[S.q[e]];
+    const float m2 = (MODE == 0 || a.mass4r) ? bo.z * 4.0f : w.body_c[id].x;
+    if (single_pair<true>(w, a, co, v2(0.0f, 0.0f), so, ro, mo, id, v2(bo.x, bo.y), bo.z, m2, sp, jown))
+      f = 1u | (sp.pushed ? 2u : 0u) | (id < co ? 4u : 0u);
+  }
+  const uint32_t at = o0 + min(rank, okk - 1u);
+  S.cx[at] = sp.corr.x;
+  S.cy[at] = sp.corr.y;
+  S.fl[at] = (uint8_t)f;
+}
+
+// Every lane of the warp calls this; a lane with no near candidates passes
+// near = 0 and gets p back.  jbase is the slot of lane 0.
+template <int MODE>
+__device__ __forceinline__ float2 apply_near_warp(const WorldDev& w, const SingleArgs& a, PairSlots& S,
+                                                  uint32_t lane, uint32_t jbase, unsigned long long near,
+                                                  uint32_t s0, uint32_t s1, uint32_t s2, uint32_t t1, uint32_t t2,
+                                                  uint32_t c, float2 s, float r, float m, float2 p,
+                                                  uint32_t& ncontacts, uint32_t& npush) {
+  const uint32_t* __restrict__ Cw = reinterpret_cast<const uint32_t*>(a.cand);
+  const uint32_t kk = (uint32_t)__popcll(near);
+  uint32_t incl = kk;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  const uint32_t off = incl - kk;
+  for (uint32_t base = 0; base < total;) {
+    // this round: the ranges that lie wholly in [base, base + PAIR_CAP)
+    const bool mine = kk > 0u && off >= base && off + kk <= base + PAIR_CAP;
+    uint32_t end = mine ? off + kk : base;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) end = max(end, __shfl_xor_sync(0xffffffffu, end, o));
+    const uint32_t cnt = end - base, r0 = off - base;
+    if (mine) {
+      uint32_t e = r0;
+      for (unsigned long long mk = near; mk; mk &= mk - 1ull, ++e) {
+        const uint32_t tt = (uint32_t)(__ffsll((long long)mk) - 1);
+        const uint32_t q = tt < t1 ? s0 + tt : (tt < t2 ? s1 + (tt - t1) : s2 + (tt - t2));
+        S.id[e] = Cw[4u * q + 3u];
+        S.q[e] = q;
+        S.own[e] = (uint8_t)lane;
+      }
+    }
+    __syncwarp();
+    for (uint32_t e0 = 0; e0 < cnt; e0 += 32u) {
+      const uint32_t e = e0 + lane;
+      const uint32_t o = e < cnt ? (uint32_t)S.own[e] : lane;
+      const float2 so = v2(__shfl_sync(0xffffffffu, s.x, o), __shfl_sync(0xffffffffu, s.y, o));
+      const float ro = __shfl_sync(0xffffffffu, r, o), mo = __shfl_sync(0xffffffffu, m, o);
+      const uint32_t co = __shfl_sync(0xffffffffu, c, o);
+      const uint32_t o0 = __shfl_sync(0xffffffffu, r0, o), okk = __shfl_sync(0xffffffffu, kk, o);
+      if (e < cnt) shared_pair<MODE>(w, a, S, e, jbase + o, so, ro, mo, co, o0, okk);
+    }
+    __syncwarp();
+    if (mine) {
+      for (uint32_t i = r0; i < r0 + kk; ++i) {
+        const uint32_t f = S.fl[i];
+        if (!(f & 1u)) continue;
+        if (f & 2u) p = add(p, (f & 4u) ? v2(0.01f, 0.0f) : v2(-0.01f, -0.0f));
+        p = add(p, v2(S.cx[i], S.cy[i]));
+        if (f & 4u) {
+          ++ncontacts;
+          npush += (f >> 1) & 1u;
+        }
+      }
+    }
+    __syncwarp();
+    base = end;
+  }
+  return p;
+}
+
 // Storage slot i -> its position in this substep's cell order.
 __global__ void __launch_bounds__(256) k_permute(WorldDev w, SingleArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -451,33 +574,47 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 // O(contacts x candidates) walk or the O(near^2) ordered selection.
 template <int MODE, bool HOOKS>
 __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, SingleArgs a) {
-  // phase 2 slots of the plain step: near candidate ids and positions,
+  // phase 2 shared out over the warp (apply_near_warp): the plain step of a
+  // uniform world
+  constexpr bool WARP2 = MODE == 0 && !HOOKS;
+  // phase 2 of the others: near candidate ids and positions,
   // thread-interleaved
-  __shared__ uint32_t s_ids[DEFER_NEAR * STEP_THREADS], s_qs[DEFER_NEAR * STEP_THREADS];
+  __shared__ uint32_t s_ids[WARP2 ? 1 : DEFER_NEAR * STEP_THREADS], s_qs[WARP2 ? 1 : DEFER_NEAR * STEP_THREADS];
   // event stream: the partners of this thread's events of phase 2, appended
   // together by the warp after it
   __shared__ uint32_t s_ev[HOOKS ? DEFER_NEAR * STEP_THREADS : 1];
+  // the near pairs of each warp
+  __shared__ PairSlots s_pairs[WARP2 ? STEP_THREADS / 32 : 1];
   uint32_t nev = 0;
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
+  const bool live = j < w.n_bodies;
   uint32_t ncontacts = 0, npush = 0;
   bool deferred = false;  // contacts (and the rest of the body's substep) left to k_step_deferred
-  if (j < w.n_bodies) {
-    const float4 av = a.a_in[j];
-    const float4 bv = a.b_in[j];
-    uint32_t c = __float_as_uint(av.w);
+  // this lane's near candidates for the warp's phase 2
+  unsigned long long wnear = 0ull;
+  uint32_t ws0 = 0, ws1 = 0, ws2 = 0, wt1 = 0, wt2 = 0;
+  float4 av = make_float4(0.0f, 0.0f, 0.0f, 0.0f), bv = av;
+  uint32_t c = 0;
+  const WorldParam wp0 = w.wparam[0];
+  BodyConst k;
+  k.m = 0.0f;
+  float2 p0 = v2(0.0f, 0.0f), p = p0;
+  uint32_t nrec = 0;  // contacts recorded for the adjoint
+  if (live) {
+    av = a.a_in[j];
+    bv = a.b_in[j];
+    c = __float_as_uint(av.w);
     if (c >= w.n_bodies) {
       atomicOr(w.status, ST_BAD_INDEX);
       c = 0;
     }
     const float2 s = v2(av.x, av.y);
     const float r = av.z;
-    const WorldParam wp0 = w.wparam[0];
-    const BodyConst k = body_const<MODE>(w, wp0, c, r);
+    k = body_const<MODE>(w, wp0, c, r);
     const WorldParam wp = MODE == 2 ? w.wparam[k.world] : wp0;
-    const float2 p0 = v2(bv.x, bv.y);  // position at the start of the substep
-    float2 p = p0;
-    uint32_t nrec = 0;  // contacts recorded for the adjoint
+    p0 = v2(bv.x, bv.y);  // position at the start of the substep
+    p = p0;
 
     const uint32_t own_key = a.contacts ? a.own_cell[j] : 0u;
     const uint32_t wm = (1u << wp.log2w) - 1u, hm = (1u << wp.log2h) - 1u;
@@ -506,10 +643,20 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
         const uint32_t t2 = t;
         near_range(C, s, r, c, s2, s2 + l2, t, nb);
         // Phase 2: the near candidates in ascending arena id
-        if (__popcll(nb) > DEFER_NEAR) deferred = true;
-        else p = apply_near_s<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec,
-                                           s_ids + threadIdx.x, s_qs + threadIdx.x, s_ev + (HOOKS ? threadIdx.x : 0u),
-                                           nev);
+        if ((uint32_t)__popcll(nb) > (WARP2 ? WARP_NEAR : DEFER_NEAR)) {
+          deferred = true;
+        } else if (!WARP2) {
+          p = apply_near_s<MODE, HOOKS>(w, a, nb, s0, s1, s2, t1, t2, j, c, p0, s, r, k.m, ncontacts, npush, nrec,
+                                        s_ids + threadIdx.x, s_qs + threadIdx.x,
+                                        s_ev + (HOOKS ? threadIdx.x : 0u), nev);
+        } else {
+          wnear = nb;
+          ws0 = s0;
+          ws1 = s1;
+          ws2 = s2;
+          wt1 = t1;
+          wt2 = t2;
+        }
       } else {
         deferred = true;
       }
@@ -565,12 +712,21 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
         deferred = true;
       }
     }
-
-    if (HOOKS && a.rec_list && !deferred) {
-      a.rec_n[c] = nrec;
-      if (nrec) atomicMax(a.rec_max, nrec);
+    if (!WARP2 && !deferred) {
+      if (HOOKS && a.rec_list) {
+        a.rec_n[c] = nrec;
+        if (nrec) atomicMax(a.rec_max, nrec);
+      }
+      finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
     }
-    if (!deferred) finish_single<MODE>(w, a, wp, k, j, c, av, bv, p0, p);
+  }
+  if (WARP2) {
+    if (a.contacts)
+      p = apply_near_warp<MODE>(w, a, s_pairs[threadIdx.x >> 5], lane, j - lane, wnear, ws0, ws1, ws2, wt1, wt2, c,
+                                v2(av.x, av.y), av.z, k.m, p, ncontacts, npush);
+    // the records again (cache hits) rather than registers held across
+    // phase 2
+    if (live && !deferred) finish_single<MODE>(w, a, wp0, k, j, c, a.a_in[j], a.b_in[j], p0, p);
   }
   if (HOOKS && w.ev_rec) {
     // phase 2's events of the warp: one atomic for all of them
