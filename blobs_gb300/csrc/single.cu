@@ -746,18 +746,29 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
       const uint32_t seq = *w.ev_seq;
       const uint32_t c = __float_as_uint(a.a_in[j].w);
       const float2 va = a.v_in[j];
-      for (uint32_t i = 0; i < nev; ++i) {
-        const uint32_t slot = base + (incl - nev) + i;
-        const uint32_t lo = s_ev[i * STEP_THREADS + threadIdx.x];
-        const uint32_t jl = w.where[lo];
-        if (jl >= w.n_bodies) {
-          atomicOr(w.status, ST_BAD_INDEX);
-          continue;
-        }
-        if (slot < w.ev_cap) {
-          const float2 vb = a.v_in[jl];
-          w.ev_rec[slot] = make_uint4(seq, c, lo, 0u);
-          w.ev_vel[slot] = make_float4(va.x, va.y, vb.x, vb.y);
+      // four events at a time: their partners' slot and velocity loads in
+      // flight together
+      for (uint32_t i0 = 0; i0 < nev; i0 += 4u) {
+        uint32_t lo[4], jl[4];
+        float2 vb[4];
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) lo[u] = i0 + u < nev ? s_ev[(i0 + u) * STEP_THREADS + threadIdx.x] : 0u;
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) jl[u] = i0 + u < nev ? w.where[lo[u]] : 0u;
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) vb[u] = i0 + u < nev && jl[u] < w.n_bodies ? a.v_in[jl[u]] : v2(0.0f, 0.0f);
+#pragma unroll
+        for (uint32_t u = 0; u < 4u; ++u) {
+          if (i0 + u >= nev) break;
+          const uint32_t slot = base + (incl - nev) + i0 + u;
+          if (jl[u] >= w.n_bodies) {
+            atomicOr(w.status, ST_BAD_INDEX);
+            continue;
+          }
+          if (slot < w.ev_cap) {
+            w.ev_rec[slot] = make_uint4(seq, c, lo[u], 0u);
+            w.ev_vel[slot] = make_float4(va.x, va.y, vb[u].x, vb[u].y);
+          }
         }
       }
     }
@@ -848,6 +859,29 @@ __global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, Sin
         S.order[rank] = e;
       }
       __syncwarp();
+      if (HOOKS && w.ev_rec) {
+        // the body's events (its contacts with lower ids), appended by all
+        // lanes; the host puts the buffer in the reference's order
+        const uint32_t seq = *w.ev_seq;
+        const float2 va = a.v_in[j];
+        for (uint32_t e0 = 0; e0 < cnt; e0 += 32u) {
+          const uint32_t e = e0 + lane;
+          const uint32_t c2 = e < cnt ? S.id[e] : 0xffffffffu;
+          const bool ev = c2 < c;
+          const uint32_t jl = ev ? w.where[c2] : 0u;
+          const uint32_t bal = __ballot_sync(0xffffffffu, ev);
+          uint32_t base = 0;
+          if (lane == 0 && bal) base = atomicAdd(w.ev_count, (uint32_t)__popc(bal));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          const uint32_t slot = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+          if (ev && jl >= n) atomicOr(w.status, ST_BAD_INDEX);
+          if (ev && slot < w.ev_cap) {
+            const float2 vb = jl < n ? a.v_in[jl] : v2(0.0f, 0.0f);
+            w.ev_rec[slot] = make_uint4(seq, c, c2, 0u);
+            w.ev_vel[slot] = make_float4(va.x, va.y, vb.x, vb.y);
+          }
+        }
+      }
       if (lane == 0) {
         float2 p = p0;
         uint32_t nrec = 0;
@@ -866,7 +900,6 @@ __global__ void __launch_bounds__(DEFER_THREADS) k_step_deferred(WorldDev w, Sin
           if (c2 < c) {
             ++tc;
             tp += pushed ? 1u : 0u;
-            if (HOOKS && w.ev_rec) single_event(w, a, c, j, c2);
           }
         }
         if (HOOKS && a.rec_list) {
