@@ -721,7 +721,8 @@ __global__ void __launch_bounds__(STEP_THREADS, 8) k_step_single(WorldDev w, Sin
     }
   }
   if (WARP2) {
-    if (a.contacts)
+    // (a warp without near candidates skips phase 2)
+    if (a.contacts && __any_sync(0xffffffffu, wnear != 0ull))
       p = apply_near_warp<MODE>(w, a, s_pairs[threadIdx.x >> 5], lane, j - lane, wnear, ws0, ws1, ws2, wt1, wt2, c,
                                 v2(av.x, av.y), av.z, k.m, p, ncontacts, npush);
     // the records again (cache hits) rather than registers held across
