@@ -373,8 +373,9 @@ __device__ __forceinline__ void finish_single(const WorldDev& w, const SingleArg
 }
 
 
-// Phase 2 of the plain step (at most DEFER_NEAR near candidates): the near
-// candidates' ids are gathered into this thread's shared-memory slots first
+// Phase 2 per lane (the event, recording and per-body-record variants; at
+// most DEFER_NEAR near candidates): the near candidates' ids are gathered
+// into this thread's shared-memory slots first
 // (independent loads), then the ascending-id selection runs over shared
 // memory and only the chosen candidate's record is loaded again.
 template <int MODE, bool HOOKS>
@@ -569,7 +570,8 @@ __global__ void __launch_bounds__(256) k_scatter_cand(WorldDev w, const float4* 
 
 // HOOKS: compiled with the adjoint's contact recording and the collision
 // event stream.  A body whose 3x3 cells hold too many candidates for its
-// near mask, or which has more than DEFER_NEAR near candidates, is left to
+// near mask, or which has more near candidates than its phase 2 takes
+// (WARP_NEAR shared over the warp, DEFER_NEAR per lane), is left to
 // k_step_deferred: one such body would hold its whole warp in the
 // O(contacts x candidates) walk or the O(near^2) ordered selection.
 template <int MODE, bool HOOKS>

@@ -227,7 +227,8 @@ int blobs_world_contact_count(blobs_world* w, uint64_t* total, uint64_t* last_su
 int blobs_world_pushout_count(blobs_world* w, uint64_t* total);
 /* No counterpart in the reference (a cost diagnostic): bodies of the
  * single-sphere path whose 3x3 cells held more than 64 candidates, or which
- * had more than 12 near candidates, and whose contacts were therefore
+ * had more near candidates than the step kernel takes (32 in the plain step
+ * of a uniform world, 12 otherwise), and whose contacts were therefore
  * resolved by a warp of their own -- since load and in the last substep. */
 int blobs_world_deferred_count(blobs_world* w, uint64_t* total, uint64_t* last_substep);
 /* The broadphase output for the current collider snapshots: every collider
