@@ -1,0 +1,204 @@
+"""The oracle's step against a second, independent restatement of the
+reference's substep loop, written here line by line in NumPy float32
+scalars (every operation rounds to f32, none is fused, as in the Rust
+source): Physics::step -> integrate (physics.rs:78-82, :397-422) with
+apply_gravity (:369-375), brute_force_collisions (:241-317, push-out branch
+and snapshot refresh included), update_objects (:323-367, the old_dt quirk
+included) and apply_constraints (:377-395), plus the axis-aligned wall
+extension after the constraints.  Single-sphere bodies at offset zero, the
+default groups, no sensors, springs or joints.
+
+The oracle and this restatement share no code; agreeing bit for bit over
+several steps of overlapping worlds (three-way and coincident contacts,
+velocity requests, static bodies, a circle constraint, walls) pins the
+oracle's order of operations to the reference's.
+"""
+import numpy as np
+import pytest
+
+from blobs_gb300 import scenes
+from oracle import oracle
+
+F = np.float32
+
+
+def _len(x, y):
+    # glam Vec2::length: (x*x + y*y).sqrt()
+    return np.sqrt(F(x * x) + F(y * y))
+
+
+class RefWorld:
+    """The reference Physics for single-sphere bodies, in f32 scalars."""
+
+    def __init__(self, s):
+        n = s.n_bodies
+        self.n = n
+        self.pos = [[F(v) for v in row] for row in s.pos]
+        self.pos_old = [list(r) for r in self.pos]
+        self.vreq = [([F(v) for v in s.vreq[i]] if s.vreq_set[i] else None) for i in range(n)]
+        self.static = [bool(s.body_type[i] == 1) for i in range(n)]
+        self.gmod = [F(v) for v in s.gravity_mod]
+        self.r = [F(v) for v in s.col_radius]
+        # rigid_body.rs:96-128 with collider.rs:40-42: the handle is listed
+        # twice, each adds mass = radius * 2
+        self.m = [F(F(F(0.0) + F(r * F(2.0))) + F(r * F(2.0))) for r in self.r]
+        # the collider's absolute translation: body transform * offset(0)
+        self.snap = [[F(F(0.0) + p[0]), F(F(0.0) + p[1])] for p in self.pos]
+        self.vel = [[F(0.0), F(0.0)] for _ in range(n)]
+        self.g = [F(v) for v in s.gravity]
+        self.old_dt = F(1.0)  # Physics::new
+        self.circles = [[F(v) for v in c] for c in s.circles]
+        self.box = [F(v) for v in s.world_box[0]] if s.world_box is not None and len(s.world_box) else None
+        self.contacts = 0
+
+    def step(self, delta):
+        dt_total = F(delta)                      # delta as f32
+        dt = F(dt_total / F(8.0))                # integrate: delta / substeps
+        for _ in range(8):
+            acc = [[F(0.0), F(0.0)] for _ in range(self.n)]
+            for i in range(self.n):             # apply_gravity
+                if not self.static[i]:
+                    acc[i][0] = F(acc[i][0] + F(self.g[0] * self.gmod[i]))
+                    acc[i][1] = F(acc[i][1] + F(self.g[1] * self.gmod[i]))
+            self._collisions()
+            self._update_objects(dt, acc)
+            self._constraints()
+
+    def _collisions(self):
+        P, S = self.pos, self.snap
+        for a in range(self.n):                 # idx_a, then idx_b among the earlier keys
+            for b in range(a):
+                ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
+                dist = _len(ax, ay)
+                min_dist = F(self.r[a] + self.r[b])
+                if not dist < min_dist:
+                    continue
+                if dist < F(1e-6):
+                    P[a][0] = F(P[a][0] + F(0.01))
+                    P[a][1] = F(P[a][1] + F(0.0))
+                    P[b][0] = F(P[b][0] - F(0.01))
+                    P[b][1] = F(P[b][1] - F(0.0))
+                    S[a] = [F(P[a][0] + F(0.0)), F(P[a][1] + F(0.0))]  # position + offset translation
+                    S[b] = [F(P[b][0] + F(0.0)), F(P[b][1] + F(0.0))]
+                    ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
+                    dist = _len(ax, ay)
+                nx, ny = F(ax / dist), F(ay / dist)
+                delta = F(min_dist - dist)
+                ratio = F(F(1.0) - F(self.m[a] / F(self.m[a] + self.m[b])))
+                ka = F(ratio * delta)
+                P[a][0] = F(P[a][0] + F(ka * nx))
+                P[a][1] = F(P[a][1] + F(ka * ny))
+                kb = F(F(F(1.0) - ratio) * delta)
+                P[b][0] = F(P[b][0] - F(kb * nx))
+                P[b][1] = F(P[b][1] - F(kb * ny))
+                self.contacts += 1
+
+    def _update_objects(self, dt, acc):
+        for i in range(self.n):
+            p, po = self.pos[i], self.pos_old[i]
+            if self.static[i]:
+                self.pos_old[i] = list(p)
+                self.vel[i] = [F(0.0), F(0.0)]
+                continue
+            if self.vreq[i] is not None:
+                q = self.vreq[i]
+                self.vreq[i] = None
+                po = [F(p[0] - F(q[0] * dt)), F(p[1] - F(q[1] * dt))]
+            k = F(dt / self.old_dt)
+            dx, dy = F(F(p[0] - po[0]) * k), F(F(p[1] - po[1]) * k)
+            self.old_dt = dt
+            self.pos_old[i] = list(p)
+            self.pos[i] = [F(p[0] + F(dx + F(F(acc[i][0] * dt) * dt))),
+                           F(p[1] + F(dy + F(F(acc[i][1] * dt) * dt)))]
+            self.vel[i] = [F(dx / dt), F(dy / dt)]
+        self.snap = [[F(F(0.0) + p[0]), F(F(0.0) + p[1])] for p in self.pos]
+
+    def _constraints(self):
+        for cx, cy, radius in self.circles:
+            for i in range(self.n):
+                tx, ty = F(self.pos[i][0] - cx), F(self.pos[i][1] - cy)
+                dist = _len(tx, ty)
+                if dist > radius:
+                    self.pos[i] = [F(cx + F(F(tx / dist) * radius)), F(cy + F(F(ty / dist) * radius))]
+        if self.box is not None:
+            lo_x, lo_y, hi_x, hi_y = self.box
+            for i in range(self.n):
+                r = self.r[i]
+                self.pos[i][0] = min(max(self.pos[i][0], F(lo_x + r)), F(hi_x - r))
+                self.pos[i][1] = min(max(self.pos[i][1], F(lo_y + r)), F(hi_y - r))
+
+    def bodies(self):
+        return {"pos": np.array(self.pos, np.float64), "pos_old": np.array(self.pos_old, np.float64),
+                "vel": np.array(self.vel, np.float64)}
+
+
+def _world(seed, n, walls, circle, coincident, statics):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    h = 0.9
+    pos = rng.uniform(-h, h, (n, 2)).astype(np.float32)
+    rad = rng.uniform(0.05, 0.15, n).astype(np.float32)
+    vel = rng.normal(0.0, 1.0, (n, 2)).astype(np.float32)
+    if coincident:
+        pos[7] = pos[3]  # the push-out branch (physics.rs:272-286)
+    bt = np.zeros(n, np.uint8)
+    if statics:
+        bt[::9] = 1
+    s = scenes.spheres(pos, rad, vel, box=(-1.0, -1.0, 1.0, 1.0) if walls else None, body_type=bt)
+    if circle:
+        s.circles = np.array([[0.1, -0.05, 0.8]], np.float32)
+    return s
+
+
+@pytest.mark.parametrize("seed,walls,circle,coincident,statics", [
+    (1, True, False, False, False),
+    (2, False, True, True, False),
+    (3, True, True, False, True),
+    (4, True, False, True, True),
+])
+def test_oracle_equals_the_line_by_line_restatement(seed, walls, circle, coincident, statics):
+    s = _world(seed, 48, walls, circle, coincident, statics)
+    dt, steps = 1.0 / 60.0, 3
+    ref = RefWorld(s)
+    for _ in range(steps):
+        ref.step(dt)
+    o = oracle.OracleWorld(s, 32)
+    assert o.step(dt, steps) == 0
+    got = o.bodies()
+    want = ref.bodies()
+    assert ref.contacts > 100  # overlapping worlds: many contacts each substep
+    for k in ("pos", "pos_old", "vel"):
+        assert np.array_equal(got[k], want[k]), (k, float(np.abs(got[k] - want[k]).max()))
+    assert o.contacts == ref.contacts
+    if coincident:
+        assert o.pushouts >= 1
+
+
+def test_restatement_reacts_to_the_pair_order():
+    """The restatement is sensitive to what it pins: resolving the pairs with
+    the inner index first (a different sequence) changes the result."""
+    s = _world(5, 32, True, False, False, False)
+    a = RefWorld(s)
+    a.step(1.0 / 60.0)
+    b = RefWorld(s)
+    orig = b._collisions
+
+    def swapped():
+        P, S = b.pos, b.snap
+        # same pairs, each body's partners visited in descending order
+        for a_ in range(b.n - 1, -1, -1):
+            for c in range(a_ - 1, -1, -1):
+                ax, ay = F(S[a_][0] - S[c][0]), F(S[a_][1] - S[c][1])
+                dist = _len(ax, ay)
+                md = F(b.r[a_] + b.r[c])
+                if not dist < md:
+                    continue
+                nx, ny = F(ax / dist), F(ay / dist)
+                d = F(md - dist)
+                ratio = F(F(1.0) - F(b.m[a_] / F(b.m[a_] + b.m[c])))
+                ka, kb = F(ratio * d), F(F(F(1.0) - ratio) * d)
+                P[a_][0], P[a_][1] = F(P[a_][0] + F(ka * nx)), F(P[a_][1] + F(ka * ny))
+                P[c][0], P[c][1] = F(P[c][0] - F(kb * nx)), F(P[c][1] - F(kb * ny))
+    b._collisions = swapped
+    b.step(1.0 / 60.0)
+    b._collisions = orig
+    assert not np.array_equal(a.bodies()["pos"], b.bodies()["pos"])
