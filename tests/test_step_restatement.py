@@ -3,15 +3,16 @@ reference's substep loop, written here line by line in NumPy float32
 scalars (every operation rounds to f32, none is fused, as in the Rust
 source): Physics::step -> integrate (physics.rs:78-82, :397-422) with
 apply_gravity (:369-375), brute_force_collisions (:241-317, push-out branch
-and snapshot refresh included), update_objects (:323-367, the old_dt quirk
+and snapshot refresh included), Spring::apply_force (springs.rs:25-47, the
+f32 - Vec2 broadcast included), update_objects (:323-367, the old_dt quirk
 included) and apply_constraints (:377-395), plus the axis-aligned wall
 extension after the constraints.  Single-sphere bodies at offset zero, the
-default groups, no sensors, springs or joints.
+default groups, no sensors or joints.
 
 The oracle and this restatement share no code; agreeing bit for bit over
 several steps of overlapping worlds (three-way and coincident contacts,
-velocity requests, static bodies, a circle constraint, walls) pins the
-oracle's order of operations to the reference's.
+velocity requests, static bodies, damped springs, a circle constraint,
+walls) pins the oracle's order of operations to the reference's.
 """
 import numpy as np
 import pytest
@@ -49,6 +50,8 @@ class RefWorld:
         self.old_dt = F(1.0)  # Physics::new
         self.circles = [[F(v) for v in c] for c in s.circles]
         self.box = [F(v) for v in s.world_box[0]] if s.world_box is not None and len(s.world_box) else None
+        self.springs = [(int(a), int(b), F(rest), F(k), F(c))
+                        for a, b, rest, k, c in zip(s.spr_a, s.spr_b, s.spr_rest, s.spr_k, s.spr_c)]
         self.contacts = 0
 
     def step(self, delta):
@@ -60,9 +63,31 @@ class RefWorld:
                 if not self.static[i]:
                     acc[i][0] = F(acc[i][0] + F(self.g[0] * self.gmod[i]))
                     acc[i][1] = F(acc[i][1] + F(self.g[1] * self.gmod[i]))
+            for spring in self.springs:
+                self._spring(spring, acc)
             self._collisions()
             self._update_objects(dt, acc)
             self._constraints()
+
+    def _spring(self, spring, acc):
+        a, b, rest, k, c = spring
+        pa, pb = self.pos[a], self.pos[b]
+        dx, dy = F(pb[0] - pa[0]), F(pb[1] - pa[1])
+        dist = _len(dx, dy)
+        ux, uy = F(dx / dist), F(dy / dist)
+        rvx, rvy = F(self.vel[a][0] - self.vel[b][0]), F(self.vel[a][1] - self.vel[b][1])
+        dot = F(F(rvx * ux) + F(rvy * uy))
+        cd = F(c * dot)
+        damp_x, damp_y = F(cd * ux), F(cd * uy)
+        sk = F(k * F(dist - rest))
+        mx, my = F(sk - damp_x), F(sk - damp_y)  # f32 - Vec2: the scalar minus each component
+        fx, fy = F(ux * mx), F(uy * my)
+        if not self.static[a]:  # RigidBody::apply_force: a = F / m
+            acc[a][0] = F(acc[a][0] + F(fx / self.m[a]))
+            acc[a][1] = F(acc[a][1] + F(fy / self.m[a]))
+        if not self.static[b]:
+            acc[b][0] = F(acc[b][0] + F(F(-fx) / self.m[b]))
+            acc[b][1] = F(acc[b][1] + F(F(-fy) / self.m[b]))
 
     def _collisions(self):
         P, S = self.pos, self.snap
@@ -132,7 +157,7 @@ class RefWorld:
                 "vel": np.array(self.vel, np.float64)}
 
 
-def _world(seed, n, walls, circle, coincident, statics):
+def _world(seed, n, walls, circle, coincident, statics, springs=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     h = 0.9
     pos = rng.uniform(-h, h, (n, 2)).astype(np.float32)
@@ -146,17 +171,26 @@ def _world(seed, n, walls, circle, coincident, statics):
     s = scenes.spheres(pos, rad, vel, box=(-1.0, -1.0, 1.0, 1.0) if walls else None, body_type=bt)
     if circle:
         s.circles = np.array([[0.1, -0.05, 0.8]], np.float32)
+    if springs:
+        a = rng.integers(0, n, 40)
+        b = (a + rng.integers(1, n, 40)) % n
+        s.spr_a, s.spr_b = a.astype(np.uint32), b.astype(np.uint32)
+        s.spr_rest = rng.uniform(0.1, 0.6, 40).astype(np.float32)
+        s.spr_k = rng.uniform(5.0, 80.0, 40).astype(np.float32)
+        s.spr_c = rng.uniform(0.0, 2.0, 40).astype(np.float32)
     return s
 
 
-@pytest.mark.parametrize("seed,walls,circle,coincident,statics", [
-    (1, True, False, False, False),
-    (2, False, True, True, False),
-    (3, True, True, False, True),
-    (4, True, False, True, True),
+@pytest.mark.parametrize("seed,walls,circle,coincident,statics,springs", [
+    (1, True, False, False, False, False),
+    (2, False, True, True, False, False),
+    (3, True, True, False, True, False),
+    (4, True, False, True, True, False),
+    (6, True, False, False, False, True),
+    (7, True, True, True, True, True),
 ])
-def test_oracle_equals_the_line_by_line_restatement(seed, walls, circle, coincident, statics):
-    s = _world(seed, 48, walls, circle, coincident, statics)
+def test_oracle_equals_the_line_by_line_restatement(seed, walls, circle, coincident, statics, springs):
+    s = _world(seed, 48, walls, circle, coincident, statics, springs)
     dt, steps = 1.0 / 60.0, 3
     ref = RefWorld(s)
     for _ in range(steps):
@@ -171,6 +205,14 @@ def test_oracle_equals_the_line_by_line_restatement(seed, walls, circle, coincid
     assert o.contacts == ref.contacts
     if coincident:
         assert o.pushouts >= 1
+    if springs:
+        # the springs move the result (both sides read them)
+        s.spr_a, s.spr_b = s.spr_a[:0], s.spr_b[:0]
+        s.spr_rest, s.spr_k, s.spr_c = s.spr_rest[:0], s.spr_k[:0], s.spr_c[:0]
+        bare = RefWorld(s)
+        for _ in range(steps):
+            bare.step(dt)
+        assert not np.array_equal(bare.bodies()["pos"], want["pos"])
 
 
 def test_restatement_reacts_to_the_pair_order():
