@@ -6,8 +6,9 @@ apply_gravity (:369-375), brute_force_collisions (:241-317, push-out branch
 and snapshot refresh included), Spring::apply_force (springs.rs:25-47, the
 f32 - Vec2 broadcast included), update_objects (:323-367, the old_dt quirk
 included) and apply_constraints (:377-395), plus the axis-aligned wall
-extension after the constraints.  Single-sphere bodies at offset zero, the
-default groups, no sensors or joints.
+extension after the constraints, and the CollisionEvent of every pair in
+contact (:288-311).  Single-sphere bodies at offset zero, with sensors and
+collision groups (groups.rs:52-57), no joints.
 
 The oracle and this restatement share no code; agreeing bit for bit over
 several steps of overlapping worlds (three-way and coincident contacts,
@@ -40,9 +41,14 @@ class RefWorld:
         self.static = [bool(s.body_type[i] == 1) for i in range(n)]
         self.gmod = [F(v) for v in s.gravity_mod]
         self.r = [F(v) for v in s.col_radius]
+        self.sensor = [bool(v) for v in s.col_sensor]
+        self.memb = [int(v) for v in s.col_memb]
+        self.filt = [int(v) for v in s.col_filt]
         # rigid_body.rs:96-128 with collider.rs:40-42: the handle is listed
-        # twice, each adds mass = radius * 2
-        self.m = [F(F(F(0.0) + F(r * F(2.0))) + F(r * F(2.0))) for r in self.r]
+        # twice, each adds mass = radius * 2; sensors add nothing, and a
+        # mass of 0 becomes 1
+        self.m = [F(1.0) if sn else F(F(F(0.0) + F(r * F(2.0))) + F(r * F(2.0)))
+                  for r, sn in zip(self.r, self.sensor)]
         # the collider's absolute translation: body transform * offset(0)
         self.snap = [[F(F(0.0) + p[0]), F(F(0.0) + p[1])] for p in self.pos]
         self.vel = [[F(0.0), F(0.0)] for _ in range(n)]
@@ -53,6 +59,8 @@ class RefWorld:
         self.springs = [(int(a), int(b), F(rest), F(k), F(c))
                         for a, b, rest, k, c in zip(s.spr_a, s.spr_b, s.spr_rest, s.spr_k, s.spr_c)]
         self.contacts = 0
+        self.events = []  # (a, b, impact velocity a, impact velocity b)
+        self.group_skips = 0  # pairs in range that the groups keep apart
 
     def step(self, delta):
         dt_total = F(delta)                      # delta as f32
@@ -93,6 +101,11 @@ class RefWorld:
         P, S = self.pos, self.snap
         for a in range(self.n):                 # idx_a, then idx_b among the earlier keys
             for b in range(a):
+                # InteractionGroups::test, both ways
+                if not (self.memb[a] & self.filt[b] and self.memb[b] & self.filt[a]):
+                    if _len(F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])) < F(self.r[a] + self.r[b]):
+                        self.group_skips += 1
+                    continue
                 ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
                 dist = _len(ax, ay)
                 min_dist = F(self.r[a] + self.r[b])
@@ -107,16 +120,19 @@ class RefWorld:
                     S[b] = [F(P[b][0] + F(0.0)), F(P[b][1] + F(0.0))]
                     ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
                     dist = _len(ax, ay)
-                nx, ny = F(ax / dist), F(ay / dist)
-                delta = F(min_dist - dist)
-                ratio = F(F(1.0) - F(self.m[a] / F(self.m[a] + self.m[b])))
-                ka = F(ratio * delta)
-                P[a][0] = F(P[a][0] + F(ka * nx))
-                P[a][1] = F(P[a][1] + F(ka * ny))
-                kb = F(F(F(1.0) - ratio) * delta)
-                P[b][0] = F(P[b][0] - F(kb * nx))
-                P[b][1] = F(P[b][1] - F(kb * ny))
+                impact = (list(self.vel[a]), list(self.vel[b]))
+                if not self.sensor[a] and not self.sensor[b]:
+                    nx, ny = F(ax / dist), F(ay / dist)
+                    delta = F(min_dist - dist)
+                    ratio = F(F(1.0) - F(self.m[a] / F(self.m[a] + self.m[b])))
+                    ka = F(ratio * delta)
+                    P[a][0] = F(P[a][0] + F(ka * nx))
+                    P[a][1] = F(P[a][1] + F(ka * ny))
+                    kb = F(F(F(1.0) - ratio) * delta)
+                    P[b][0] = F(P[b][0] - F(kb * nx))
+                    P[b][1] = F(P[b][1] - F(kb * ny))
                 self.contacts += 1
+                self.events.append((a, b, impact[0], impact[1]))
 
     def _update_objects(self, dt, acc):
         for i in range(self.n):
@@ -157,7 +173,7 @@ class RefWorld:
                 "vel": np.array(self.vel, np.float64)}
 
 
-def _world(seed, n, walls, circle, coincident, statics, springs=False):
+def _world(seed, n, walls, circle, coincident, statics, springs=False, sensors_groups=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     h = 0.9
     pos = rng.uniform(-h, h, (n, 2)).astype(np.float32)
@@ -171,6 +187,10 @@ def _world(seed, n, walls, circle, coincident, statics, springs=False):
     s = scenes.spheres(pos, rad, vel, box=(-1.0, -1.0, 1.0, 1.0) if walls else None, body_type=bt)
     if circle:
         s.circles = np.array([[0.1, -0.05, 0.8]], np.float32)
+    if sensors_groups:
+        s.col_sensor = (np.arange(n) % 5 == 2).astype(np.uint8)
+        s.col_memb = rng.choice(np.array([1, 2, 3, 0xffffffff], np.uint32), n)
+        s.col_filt = rng.choice(np.array([1, 2, 3, 0xffffffff], np.uint32), n)
     if springs:
         a = rng.integers(0, n, 40)
         b = (a + rng.integers(1, n, 40)) % n
@@ -244,3 +264,29 @@ def test_restatement_reacts_to_the_pair_order():
     b.step(1.0 / 60.0)
     b._collisions = orig
     assert not np.array_equal(a.bodies()["pos"], b.bodies()["pos"])
+
+
+@pytest.mark.parametrize("seed,coincident", [(8, False), (9, True)])
+def test_oracle_events_sensors_and_groups_equal_the_restatement(seed, coincident):
+    """Sensors (counted and reported, never corrected, mass 1), collision
+    groups, and the event stream in the reference's order with the parents'
+    calculated_velocity as impact velocities."""
+    s = _world(seed, 48, True, False, coincident, True, True, sensors_groups=True)
+    dt, steps = 1.0 / 60.0, 3
+    ref = RefWorld(s)
+    for _ in range(steps):
+        ref.step(dt)
+    o = oracle.OracleWorld(s, 32, record_events=True)
+    assert o.step(dt, steps) == 0
+    got, want = o.bodies(), ref.bodies()
+    for k in ("pos", "pos_old", "vel"):
+        assert np.array_equal(got[k], want[k]), (k, float(np.abs(got[k] - want[k]).max()))
+    a, b, va, vb = o.events()
+    assert len(a) == len(ref.events) == ref.contacts == o.contacts and len(a) > 100
+    assert np.array_equal(a, [e[0] for e in ref.events]) and np.array_equal(b, [e[1] for e in ref.events])
+    assert np.array_equal(va, np.array([e[2] for e in ref.events], np.float64))
+    assert np.array_equal(vb, np.array([e[3] for e in ref.events], np.float64))
+    # sensors and groups both bite: some reported pairs are not corrected,
+    # some pairs in range are not reported
+    assert any(ref.sensor[e[0]] or ref.sensor[e[1]] for e in ref.events)
+    assert ref.group_skips > 0
