@@ -7,14 +7,18 @@ and snapshot refresh included), Spring::apply_force (springs.rs:25-47, the
 f32 - Vec2 broadcast included), update_objects (:323-367, the old_dt quirk
 included) and apply_constraints (:377-395), plus the axis-aligned wall
 extension after the constraints, and the CollisionEvent of every pair in
-contact (:288-311).  Single-sphere bodies at offset zero, with sensors and
-collision groups (groups.rs:52-57), no joints.
+contact (:288-311), and solve_fixed_joints (:424-477, atan2 through the C
+library's atan2f, which the oracle also calls).  Single-sphere bodies at
+offset zero, with sensors and collision groups (groups.rs:52-57).
 
 The oracle and this restatement share no code; agreeing bit for bit over
 several steps of overlapping worlds (three-way and coincident contacts,
 velocity requests, static bodies, damped springs, a circle constraint,
 walls) pins the oracle's order of operations to the reference's.
 """
+import ctypes
+import ctypes.util
+
 import numpy as np
 import pytest
 
@@ -22,6 +26,15 @@ from blobs_gb300 import scenes
 from oracle import oracle
 
 F = np.float32
+
+_libm = ctypes.CDLL(ctypes.util.find_library("m"))
+_libm.atan2f.restype = ctypes.c_float
+_libm.atan2f.argtypes = [ctypes.c_float, ctypes.c_float]
+
+
+def _atan2(y, x):
+    """f32::atan2 (the C library's atan2f)."""
+    return F(_libm.atan2f(float(y), float(x)))
 
 
 def _len(x, y):
@@ -61,6 +74,10 @@ class RefWorld:
         self.contacts = 0
         self.events = []  # (a, b, impact velocity a, impact velocity b)
         self.group_skips = 0  # pairs in range that the groups keep apart
+        self.rot = [F(v) for v in s.rotation]
+        self.joints = [(int(a), int(b), [F(v) for v in aa], [F(v) for v in ab], F(d), F(t))
+                       for a, b, aa, ab, d, t in zip(s.jnt_a, s.jnt_b, s.jnt_anchor_a, s.jnt_anchor_b,
+                                                     s.jnt_distance, s.jnt_target)]
 
     def step(self, delta):
         dt_total = F(delta)                      # delta as f32
@@ -74,6 +91,7 @@ class RefWorld:
             for spring in self.springs:
                 self._spring(spring, acc)
             self._collisions()
+            self._joints(dt)
             self._update_objects(dt, acc)
             self._constraints()
 
@@ -134,6 +152,35 @@ class RefWorld:
                 self.contacts += 1
                 self.events.append((a, b, impact[0], impact[1]))
 
+    def _joints(self, dt):
+        for _ in range(4):  # joint_iterations
+            for a, b, anc_a, anc_b, jd, target in self.joints:
+                pa, pb = self.pos[a], self.pos[b]
+                wa = [F(pa[0] + anc_a[0]), F(pa[1] + anc_a[1])]
+                wb = [F(pb[0] + anc_b[0]), F(pb[1] + anc_b[1])]
+                dx, dy = F(wb[0] - wa[0]), F(wb[1] - wa[1])
+                dist = _len(dx, dy)
+                if dist < F(1e-6):
+                    continue
+                off = F(dist - jd)
+                cx, cy = F(F(off * dx) / dist), F(F(off * dy) / dist)  # off_by * delta / distance
+                ia, ib = F(F(1.0) / self.m[a]), F(F(1.0) / self.m[b])  # recip
+                inv_sum = F(ia + ib)
+                if self.static[a]:
+                    pb[0], pb[1] = F(pb[0] - F(inv_sum * cx)), F(pb[1] - F(inv_sum * cy))
+                elif self.static[b]:
+                    pa[0], pa[1] = F(pa[0] + F(inv_sum * cx)), F(pa[1] + F(inv_sum * cy))
+                else:
+                    ratio = F(ia / inv_sum)
+                    pa[0], pa[1] = F(pa[0] + F(ratio * cx)), F(pa[1] + F(ratio * cy))
+                    q = F(F(1.0) - ratio)
+                    pb[0], pb[1] = F(pb[0] - F(q * cx)), F(pb[1] - F(q * cy))
+                ang_a = _atan2(dy, dx)
+                ang_b = F(-_atan2(dy, F(-dx)))
+                corr = F(F(F(ang_b - ang_a) - target) * F(0.5))
+                self.rot[a] = F(self.rot[a] + F(corr * dt))
+                self.rot[b] = F(self.rot[b] - F(corr * dt))
+
     def _update_objects(self, dt, acc):
         for i in range(self.n):
             p, po = self.pos[i], self.pos_old[i]
@@ -170,10 +217,10 @@ class RefWorld:
 
     def bodies(self):
         return {"pos": np.array(self.pos, np.float64), "pos_old": np.array(self.pos_old, np.float64),
-                "vel": np.array(self.vel, np.float64)}
+                "vel": np.array(self.vel, np.float64), "rotation": np.array(self.rot, np.float64)}
 
 
-def _world(seed, n, walls, circle, coincident, statics, springs=False, sensors_groups=False):
+def _world(seed, n, walls, circle, coincident, statics, springs=False, sensors_groups=False, joints=False):
     rng = np.random.Generator(np.random.PCG64(seed))
     h = 0.9
     pos = rng.uniform(-h, h, (n, 2)).astype(np.float32)
@@ -191,6 +238,11 @@ def _world(seed, n, walls, circle, coincident, statics, springs=False, sensors_g
         s.col_sensor = (np.arange(n) % 5 == 2).astype(np.uint8)
         s.col_memb = rng.choice(np.array([1, 2, 3, 0xffffffff], np.uint32), n)
         s.col_filt = rng.choice(np.array([1, 2, 3, 0xffffffff], np.uint32), n)
+    if joints:
+        # chains of four and pairs, anchors off the centres, some to static bodies
+        a = np.array([1, 2, 3, 10, 20, 27, 30, 40], np.uint32)
+        b = np.array([2, 3, 4, 11, 21, 28, 31, 41], np.uint32)
+        scenes.add_fixed_joints(s, a, b, rng.uniform(-0.05, 0.05, (8, 2)), rng.uniform(-0.05, 0.05, (8, 2)))
     if springs:
         a = rng.integers(0, n, 40)
         b = (a + rng.integers(1, n, 40)) % n
@@ -290,3 +342,23 @@ def test_oracle_events_sensors_and_groups_equal_the_restatement(seed, coincident
     # some pairs in range are not reported
     assert any(ref.sensor[e[0]] or ref.sensor[e[1]] for e in ref.events)
     assert ref.group_skips > 0
+
+
+@pytest.mark.parametrize("seed,statics", [(10, False), (11, True)])
+def test_oracle_fixed_joints_equal_the_restatement(seed, statics):
+    """Fixed joints between single-sphere bodies (anchors not rotated, as in
+    the reference), swept 4 times per substep in arena order; positions and
+    rotations equal the oracle's bit for bit."""
+    s = _world(seed, 48, True, False, False, statics, True, joints=True)
+    dt, steps = 1.0 / 60.0, 3
+    ref = RefWorld(s)
+    for _ in range(steps):
+        ref.step(dt)
+    o = oracle.OracleWorld(s, 32)
+    assert o.step(dt, steps) == 0
+    got, want = o.bodies(), ref.bodies()
+    for k in ("pos", "pos_old", "vel", "rotation"):
+        assert np.array_equal(got[k], want[k]), (k, float(np.abs(got[k] - want[k]).max()))
+    assert np.abs(want["rotation"]).max() > 1e-3  # the joints turned the bodies
+    if statics:
+        assert any(ref.static[j[0]] or ref.static[j[1]] for j in ref.joints)
