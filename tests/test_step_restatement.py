@@ -30,11 +30,22 @@ F = np.float32
 _libm = ctypes.CDLL(ctypes.util.find_library("m"))
 _libm.atan2f.restype = ctypes.c_float
 _libm.atan2f.argtypes = [ctypes.c_float, ctypes.c_float]
+for _fn in (_libm.sinf, _libm.cosf):
+    _fn.restype = ctypes.c_float
+    _fn.argtypes = [ctypes.c_float]
 
 
 def _atan2(y, x):
     """f32::atan2 (the C library's atan2f)."""
     return F(_libm.atan2f(float(y), float(x)))
+
+
+def _sinf(x):
+    return F(_libm.sinf(float(x)))
+
+
+def _cosf(x):
+    return F(_libm.cosf(float(x)))
 
 
 def _len(x, y):
@@ -43,41 +54,69 @@ def _len(x, y):
 
 
 class RefWorld:
-    """The reference Physics for single-sphere bodies, in f32 scalars."""
+    """The reference Physics in f32 scalars: bodies in arena order, each
+    with its colliders (handles listed twice, physics.rs:144 and
+    collider.rs:180), colliders in arena order."""
 
     def __init__(self, s):
-        n = s.n_bodies
-        self.n = n
+        n, nc = s.n_bodies, len(s.col_parent)
+        self.n, self.nc = n, nc
         self.pos = [[F(v) for v in row] for row in s.pos]
         self.pos_old = [list(r) for r in self.pos]
         self.vreq = [([F(v) for v in s.vreq[i]] if s.vreq_set[i] else None) for i in range(n)]
         self.static = [bool(s.body_type[i] == 1) for i in range(n)]
         self.gmod = [F(v) for v in s.gravity_mod]
+        self.rot = [F(v) for v in s.rotation]
+        self.vel = [[F(0.0), F(0.0)] for _ in range(n)]
+        self.parent = [int(v) for v in s.col_parent]
+        self.off = [[F(v) for v in o] for o in s.col_offset]
         self.r = [F(v) for v in s.col_radius]
         self.sensor = [bool(v) for v in s.col_sensor]
         self.memb = [int(v) for v in s.col_memb]
         self.filt = [int(v) for v in s.col_filt]
-        # rigid_body.rs:96-128 with collider.rs:40-42: the handle is listed
-        # twice, each adds mass = radius * 2; sensors add nothing, and a
-        # mass of 0 becomes 1
-        self.m = [F(1.0) if sn else F(F(F(0.0) + F(r * F(2.0))) + F(r * F(2.0)))
-                  for r, sn in zip(self.r, self.sensor)]
-        # the collider's absolute translation: body transform * offset(0)
-        self.snap = [[F(F(0.0) + p[0]), F(F(0.0) + p[1])] for p in self.pos]
-        self.vel = [[F(0.0), F(0.0)] for _ in range(n)]
+        self.mass_override = [None if np.isnan(v) else F(v) for v in s.col_mass_override]
+        self.cols = [[] for _ in range(n)]
+        for c in range(nc):
+            self.cols[self.parent[c]] += [c, c]
+        # rigid_body.rs:96-128 with collider.rs:40-42: mass_override or
+        # radius * 2 per listed handle, sensors add nothing, a total of 0
+        # becomes 1
+        self.m = []
+        for i in range(n):
+            m = F(0.0)
+            for c in self.cols[i]:
+                if not self.sensor[c]:
+                    mc = self.mass_override[c]
+                    m = F(m + (F(self.r[c] * F(2.0)) if mc is None else mc))
+            self.m.append(F(1.0) if m == F(0.0) else m)
+        # the wall extension's bounding radius: max |offset| + radius
+        self.bound = [F(0.0)] * n
+        for c in range(nc):
+            self.bound[self.parent[c]] = max(self.bound[self.parent[c]], F(_len(*self.off[c]) + self.r[c]))
+        if s.col_snap is not None:
+            self.snap = [[F(v) for v in row] for row in s.col_snap]
+        else:
+            self.snap = [self._xform(self.parent[c], c) for c in range(nc)]
         self.g = [F(v) for v in s.gravity]
         self.old_dt = F(1.0)  # Physics::new
         self.circles = [[F(v) for v in c] for c in s.circles]
         self.box = [F(v) for v in s.world_box[0]] if s.world_box is not None and len(s.world_box) else None
         self.springs = [(int(a), int(b), F(rest), F(k), F(c))
                         for a, b, rest, k, c in zip(s.spr_a, s.spr_b, s.spr_rest, s.spr_k, s.spr_c)]
-        self.contacts = 0
-        self.events = []  # (a, b, impact velocity a, impact velocity b)
-        self.group_skips = 0  # pairs in range that the groups keep apart
-        self.rot = [F(v) for v in s.rotation]
         self.joints = [(int(a), int(b), [F(v) for v in aa], [F(v) for v in ab], F(d), F(t))
                        for a, b, aa, ab, d, t in zip(s.jnt_a, s.jnt_b, s.jnt_anchor_a, s.jnt_anchor_b,
                                                      s.jnt_distance, s.jnt_target)]
+        self.contacts = 0
+        self.events = []  # (a, b, impact velocity a, impact velocity b)
+        self.group_skips = 0  # pairs in range that the groups keep apart
+
+    def _xform(self, i, c):
+        """(body.transform() * collider.offset).translation: Mat2::from_angle
+        columns (cos, sin), (-sin, cos) times the offset, plus the position."""
+        sn, cs = _sinf(self.rot[i]), _cosf(self.rot[i])
+        ox, oy = self.off[c]
+        p = self.pos[i]
+        return [F(F(F(cs * ox) + F(F(-sn) * oy)) + p[0]), F(F(F(sn * ox) + F(cs * oy)) + p[1])]
 
     def step(self, delta):
         dt_total = F(delta)                      # delta as f32
@@ -117,12 +156,15 @@ class RefWorld:
 
     def _collisions(self):
         P, S = self.pos, self.snap
-        for a in range(self.n):                 # idx_a, then idx_b among the earlier keys
+        for a in range(self.nc):                # idx_a, then idx_b among the earlier keys
             for b in range(a):
                 # InteractionGroups::test, both ways
                 if not (self.memb[a] & self.filt[b] and self.memb[b] & self.filt[a]):
                     if _len(F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])) < F(self.r[a] + self.r[b]):
                         self.group_skips += 1
+                    continue
+                ia, ib = self.parent[a], self.parent[b]
+                if ia == ib:                    # colliders share a rigid body
                     continue
                 ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
                 dist = _len(ax, ay)
@@ -130,25 +172,26 @@ class RefWorld:
                 if not dist < min_dist:
                     continue
                 if dist < F(1e-6):
-                    P[a][0] = F(P[a][0] + F(0.01))
-                    P[a][1] = F(P[a][1] + F(0.0))
-                    P[b][0] = F(P[b][0] - F(0.01))
-                    P[b][1] = F(P[b][1] - F(0.0))
-                    S[a] = [F(P[a][0] + F(0.0)), F(P[a][1] + F(0.0))]  # position + offset translation
-                    S[b] = [F(P[b][0] + F(0.0)), F(P[b][1] + F(0.0))]
+                    P[ia][0] = F(P[ia][0] + F(0.01))
+                    P[ia][1] = F(P[ia][1] + F(0.0))
+                    P[ib][0] = F(P[ib][0] - F(0.01))
+                    P[ib][1] = F(P[ib][1] - F(0.0))
+                    # position + offset translation (not rotated)
+                    S[a] = [F(P[ia][0] + self.off[a][0]), F(P[ia][1] + self.off[a][1])]
+                    S[b] = [F(P[ib][0] + self.off[b][0]), F(P[ib][1] + self.off[b][1])]
                     ax, ay = F(S[a][0] - S[b][0]), F(S[a][1] - S[b][1])
                     dist = _len(ax, ay)
-                impact = (list(self.vel[a]), list(self.vel[b]))
+                impact = (list(self.vel[ia]), list(self.vel[ib]))
                 if not self.sensor[a] and not self.sensor[b]:
                     nx, ny = F(ax / dist), F(ay / dist)
                     delta = F(min_dist - dist)
-                    ratio = F(F(1.0) - F(self.m[a] / F(self.m[a] + self.m[b])))
+                    ratio = F(F(1.0) - F(self.m[ia] / F(self.m[ia] + self.m[ib])))
                     ka = F(ratio * delta)
-                    P[a][0] = F(P[a][0] + F(ka * nx))
-                    P[a][1] = F(P[a][1] + F(ka * ny))
+                    P[ia][0] = F(P[ia][0] + F(ka * nx))
+                    P[ia][1] = F(P[ia][1] + F(ka * ny))
                     kb = F(F(F(1.0) - ratio) * delta)
-                    P[b][0] = F(P[b][0] - F(kb * nx))
-                    P[b][1] = F(P[b][1] - F(kb * ny))
+                    P[ib][0] = F(P[ib][0] - F(kb * nx))
+                    P[ib][1] = F(P[ib][1] - F(kb * ny))
                 self.contacts += 1
                 self.events.append((a, b, impact[0], impact[1]))
 
@@ -198,8 +241,11 @@ class RefWorld:
             self.pos_old[i] = list(p)
             self.pos[i] = [F(p[0] + F(dx + F(F(acc[i][0] * dt) * dt))),
                            F(p[1] + F(dy + F(F(acc[i][1] * dt) * dt)))]
+            # no torque: angular_velocity and rotation keep their values
             self.vel[i] = [F(dx / dt), F(dy / dt)]
-        self.snap = [[F(F(0.0) + p[0]), F(F(0.0) + p[1])] for p in self.pos]
+        for i in range(self.n):
+            for c in self.cols[i]:
+                self.snap[c] = self._xform(i, c)
 
     def _constraints(self):
         for cx, cy, radius in self.circles:
@@ -211,7 +257,7 @@ class RefWorld:
         if self.box is not None:
             lo_x, lo_y, hi_x, hi_y = self.box
             for i in range(self.n):
-                r = self.r[i]
+                r = self.bound[i]
                 self.pos[i][0] = min(max(self.pos[i][0], F(lo_x + r)), F(hi_x - r))
                 self.pos[i][1] = min(max(self.pos[i][1], F(lo_y + r)), F(hi_y - r))
 
@@ -362,3 +408,61 @@ def test_oracle_fixed_joints_equal_the_restatement(seed, statics):
     assert np.abs(want["rotation"]).max() > 1e-3  # the joints turned the bodies
     if statics:
         assert any(ref.static[j[0]] or ref.static[j[1]] for j in ref.joints)
+
+
+def _multi_world(seed, n=28):
+    """Bodies of one to three colliders at offsets, some sensors and group
+    masks and mass overrides, jointed in pairs and chains (so the bodies
+    turn and the offsets rotate), springs, walls."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = scenes.empty_scene(n)
+    s.pos = rng.uniform(-0.8, 0.8, (n, 2)).astype(np.float32)
+    s.vreq = rng.normal(0.0, 1.0, (n, 2)).astype(np.float32)
+    s.vreq_set = np.ones(n, np.uint8)
+    s.body_type = (np.arange(n) % 11 == 5).astype(np.uint8)
+    k = rng.integers(1, 4, n)
+    parent = np.repeat(np.arange(n), k).astype(np.uint32)
+    nc = len(parent)
+    s.col_parent = parent
+    s.col_offset = rng.uniform(-0.12, 0.12, (nc, 2)).astype(np.float32)
+    s.col_radius = rng.uniform(0.04, 0.1, nc).astype(np.float32)
+    s.col_mass_override = np.where(rng.uniform(0, 1, nc) < 0.2, rng.uniform(0.05, 0.5, nc), np.nan).astype(np.float32)
+    s.col_sensor = (rng.uniform(0, 1, nc) < 0.15).astype(np.uint8)
+    s.col_memb = rng.choice(np.array([1, 2, 3, 0xffffffff], np.uint32), nc)
+    s.col_filt = rng.choice(np.array([1, 3, 0xffffffff, 0xffffffff], np.uint32), nc)
+    s.gravity = np.array([0.0, -9.81], np.float32)
+    s.world_box = np.array([[-1.0, -1.0, 1.0, 1.0]], np.float32)
+    a = np.array([0, 1, 2, 6, 9, 14, 15, 20, 24], np.uint32)
+    b = np.array([1, 2, 3, 7, 10, 16, 5, 21, 25], np.uint32)
+    scenes.add_fixed_joints(s, a, b, rng.uniform(-0.05, 0.05, (9, 2)), rng.uniform(-0.05, 0.05, (9, 2)))
+    sa = rng.integers(0, n, 12)
+    s.spr_a, s.spr_b = sa.astype(np.uint32), ((sa + rng.integers(1, n, 12)) % n).astype(np.uint32)
+    s.spr_rest = rng.uniform(0.1, 0.5, 12).astype(np.float32)
+    s.spr_k = rng.uniform(5.0, 50.0, 12).astype(np.float32)
+    s.spr_c = rng.uniform(0.0, 1.0, 12).astype(np.float32)
+    return s
+
+
+@pytest.mark.parametrize("seed", [12, 13])
+def test_oracle_multi_collider_bodies_equal_the_restatement(seed):
+    """The general path's semantics: colliders at rotated offsets (sinf and
+    cosf of the body's rotation), the same-body skip, mass summed over the
+    doubled handle list with overrides and sensors, the wall extension's
+    bounding radius; positions, rotations and events bit for bit."""
+    s = _multi_world(seed)
+    dt, steps = 1.0 / 60.0, 3
+    ref = RefWorld(s)
+    for _ in range(steps):
+        ref.step(dt)
+    o = oracle.OracleWorld(s, 32, record_events=True)
+    assert o.step(dt, steps) == 0
+    got, want = o.bodies(), ref.bodies()
+    for k in ("pos", "pos_old", "vel", "rotation"):
+        assert np.array_equal(got[k], want[k]), (k, float(np.abs(got[k] - want[k]).max()))
+    a, b, va, vb = o.events()
+    assert len(a) == len(ref.events) == o.contacts and len(a) > 50
+    assert np.array_equal(a, [e[0] for e in ref.events]) and np.array_equal(b, [e[1] for e in ref.events])
+    assert np.array_equal(va, np.array([e[2] for e in ref.events], np.float64))
+    assert np.array_equal(vb, np.array([e[3] for e in ref.events], np.float64))
+    assert np.abs(want["rotation"]).max() > 1e-3 and max(len(c) for c in ref.cols) == 6
+    assert np.array_equal(o.snapshots(), np.array(ref.snap, np.float64))
