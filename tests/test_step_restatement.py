@@ -412,14 +412,19 @@ def test_oracle_fixed_joints_equal_the_restatement(seed, statics):
 
 def _multi_world(seed, n=28):
     """Bodies of one to three colliders at offsets, some sensors and group
-    masks and mass overrides, jointed in pairs and chains (so the bodies
-    turn and the offsets rotate), springs, walls."""
+    masks and mass overrides, static and kinematic bodies, per-body gravity
+    scales, jointed in pairs and chains (so the bodies turn and the offsets
+    rotate), springs, walls."""
     rng = np.random.Generator(np.random.PCG64(seed))
     s = scenes.empty_scene(n)
     s.pos = rng.uniform(-0.8, 0.8, (n, 2)).astype(np.float32)
     s.vreq = rng.normal(0.0, 1.0, (n, 2)).astype(np.float32)
     s.vreq_set = np.ones(n, np.uint8)
-    s.body_type = (np.arange(n) % 11 == 5).astype(np.uint8)
+    # static bodies, and kinematic ones (RigidBodyType 2, 3: moved like
+    # dynamic ones by this loop, which only tests is_static)
+    s.body_type = np.where(np.arange(n) % 11 == 5, 1, np.where(np.arange(n) % 7 == 3, 2 + (np.arange(n) % 2), 0))
+    s.body_type = s.body_type.astype(np.uint8)
+    s.gravity_mod = rng.uniform(0.0, 2.0, n).astype(np.float32)
     k = rng.integers(1, 4, n)
     parent = np.repeat(np.arange(n), k).astype(np.uint32)
     nc = len(parent)
