@@ -3,8 +3,9 @@ oracle's final states are committed as digests
 (tests/golden/reference_pin.json), the target a Rust harness running the
 reference itself on the same generated inputs must hit.
 Here the oracle must keep reproducing them, the independent NumPy
-restatement of the substep loop must reach the same digests, and the
-generator's inputs must stay what the fixture records."""
+restatement of the substep loop must reach the same digests, the
+generator's inputs must stay what the fixture records, and the GPU step
+must reproduce them bit for bit."""
 import json
 import os
 
@@ -61,3 +62,18 @@ def test_restatement_reaches_the_pin_states(name):
     b = ref.bodies()
     assert {k: digest(b[k]) for k in ("pos", "pos_old", "vel")} == {k: want[k] for k in ("pos", "pos_old", "vel")}
     assert ref.contacts == want["contacts"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_reproduces_the_pin_states(name):
+    from blobs_gb300 import native
+    s, steps, dt = CASES[name]
+    want = fixture()[name]
+    with native.World(s) as w:
+        for _ in range(steps):
+            w.step(dt)
+        b = w.read_bodies()
+        contacts = w.contact_count()[0]
+    assert {k: digest(b[k]) for k in ("pos", "pos_old", "vel")} == {k: want[k] for k in ("pos", "pos_old", "vel")}
+    assert contacts == want["contacts"]
