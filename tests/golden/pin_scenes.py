@@ -8,7 +8,8 @@ or single IEEE f32 roundings, so a few lines of Rust generate the same bits
 (the harness is in INTEGRATION.md).  The scenes use only the reference's own
 features: no wall extension (a circle constraint keeps the bodies together
 instead), no joints (so no rotation and no libm), springs, sensors,
-collision groups, velocity requests and two-collider bodies.
+collision groups, velocity requests, two-collider bodies, static and
+kinematic bodies and per-body gravity scales.
 
     xorshift32:  x ^= x << 13; x ^= x >> 17; x ^= x << 5   (mod 2^32)
     unit():      next x, then (x >> 8) as f32 * 2^-24       (exact)
@@ -119,6 +120,15 @@ def pin_scenes():
     s = _bodies(g, 200, 2.5, 0.04, 0.1, 0.5, 2, spread=0.1)
     s.circles = np.array([[0.0, 0.0, 3.5]], np.float32)
     out.append(("pin_two_collider_200", s, 6, 1.0 / 60.0))
+
+    # RigidBodyType: Dynamic 0, Static 1, KinematicPositionBased 2,
+    # KinematicVelocityBased 3; gravity_mod drawn after all bodies
+    g = XorShift32(0xBB67AE85)
+    s = _bodies(g, 300, 2.5, 0.05, 0.15, 1.0, 1)
+    s.body_type = np.array([1 if i % 9 == 4 else (2 + i % 2 if i % 13 == 6 else 0) for i in range(300)], np.uint8)
+    s.gravity_mod = np.array([g.lerp(0.0, 2.0) for _ in range(300)], np.float32)
+    s.circles = np.array([[0.0, 0.0, 3.5]], np.float32)
+    out.append(("pin_body_types_300", s, 8, 1.0 / 60.0))
     return out
 
 
