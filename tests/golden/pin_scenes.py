@@ -7,9 +7,11 @@ scenes are built for a maintainer who has one: every input comes from a
 or single IEEE f32 roundings, so a few lines of Rust generate the same bits
 (the harness is in INTEGRATION.md).  The scenes use only the reference's own
 features: no wall extension (a circle constraint keeps the bodies together
-instead), no joints (so no rotation and no libm), springs, sensors,
-collision groups, velocity requests, two-collider bodies, static and
-kinematic bodies and per-body gravity scales.
+instead), springs, sensors, collision groups, velocity requests,
+two-collider bodies (without joints, so no rotation reaches them), static
+and kinematic bodies, per-body gravity scales, and fixed joints between
+single-collider bodies (whose rotations, through the C library's atan2f,
+do not reach the positions).
 
     xorshift32:  x ^= x << 13; x ^= x >> 17; x ^= x << 5   (mod 2^32)
     unit():      next x, then (x >> 8) as f32 * 2^-24       (exact)
@@ -129,6 +131,22 @@ def pin_scenes():
     s.gravity_mod = np.array([g.lerp(0.0, 2.0) for _ in range(300)], np.float32)
     s.circles = np.array([[0.0, 0.0, 3.5]], np.float32)
     out.append(("pin_body_types_300", s, 8, 1.0 / 60.0))
+
+    # fixed joints (Physics::create_fixed_joint after all bodies, in this
+    # order); single-collider bodies, so the rotations the joints drive do
+    # not reach the positions
+    g = XorShift32(0x3C6EF372)
+    s = _bodies(g, 200, 2.5, 0.05, 0.15, 1.0, 1)
+    ja, jb, aa, ab = [], [], [], []
+    for _ in range(40):
+        a = g.index(200)
+        b = (a + 1 + g.index(199)) % 200
+        ja.append(a), jb.append(b)
+        aa.append((g.lerp(-0.05, 0.05), g.lerp(-0.05, 0.05)))
+        ab.append((g.lerp(-0.05, 0.05), g.lerp(-0.05, 0.05)))
+    scenes.add_fixed_joints(s, ja, jb, aa, ab)
+    s.circles = np.array([[0.0, 0.0, 3.5]], np.float32)
+    out.append(("pin_joints_200", s, 8, 1.0 / 60.0))
     return out
 
 
